@@ -1,0 +1,330 @@
+"""Benchmark: device-resident parse throughput of the structural-index +
+column-materialisation path on one GB300.
+
+Workload (the csv-hash comment+quote dialect, 1 GiB, device-resident): one
+step = one fused falx_parse call that produces the structural index
+(byte-identical to the serial path), the field-byte totals and the typed
+columns u32 id, City string arena, u32 population, f64 latitude and f64
+longitude. Inputs are seeded synthetic documents with the workload's shapes
+(falx_gb300/gen.py); 1 GiB is larger than L2, so no flush is needed.
+
+--impl reference times the CPU port of the reference's parallel drivers
+(oracle/, all host threads) on a bounded sample of the same workload.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GIB = float(1 << 30)
+SCHEMA_COLS = [(0, 1), (1, 3), (3, 1), (4, 2), (5, 2)]  # u32 id, str City, u32 pop, f64 lat, f64 lon
+METRIC = "device-resident parse GiB/s vs HBM peak; learned-speculative vs plain, bit-exact"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Sample SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 6:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
+        mx = max((float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons}
+
+
+def make_input(size):
+    from falx_gb300 import gen
+
+    return gen.generate(gen.CSV_HASH, size)
+
+
+def cpu_sample(size):
+    from falx_gb300 import gen
+
+    return gen.generate(gen.CSV_HASH, size)
+
+
+def run_cpu(data, threads):
+    """One CPU step over `data`: the reference's parallel index, field bytes
+    and columns drivers (port)."""
+    import oracle
+
+    oracle.index_par(data, oracle.CSV_HASH, threads)
+    oracle.field_bytes(data, oracle.CSV_HASH, par_threads=threads)
+    oracle.parse_columns(data, oracle.CSV_HASH, SCHEMA_COLS, par_threads=threads)
+
+
+def cpu_baseline(sample_bytes, threads, budget_s=20.0):
+    data = cpu_sample(sample_bytes)
+    run_cpu(data, threads)  # warm-up
+    t0 = time.perf_counter()
+    reps = 0
+    best = None
+    while True:
+        s = time.perf_counter()
+        run_cpu(data, threads)
+        dt = time.perf_counter() - s
+        best = dt if best is None else min(best, dt)
+        reps += 1
+        if time.perf_counter() - t0 > budget_s or reps >= 5:
+            break
+    return data.size / GIB / best, data.size
+
+
+def bench_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample
+    t_total = []
+    from falx_gb300 import gen
+
+    data = gen.generate(gen.CSV_HASH, sample)
+    for _ in range(args.warmup):
+        run_cpu(data, threads)
+    for _ in range(args.steps):
+        s = time.perf_counter()
+        run_cpu(data, threads)
+        t_total.append(time.perf_counter() - s)
+    sec = sum(t_total) / len(t_total)
+    v = data.size / GIB / sec
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GiB/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": "csv_hash 1 GiB: index + field bytes + typed columns (CPU sample)",
+                       "sample_bytes": int(data.size)},
+            "cpu_baseline": {"value": round(v, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
+                             "sample": "%d-byte csv_hash document, full index + field bytes + columns" % data.size},
+            "e2e": {"value": round(v, 4), "unit": "GiB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def bench_gpu(args):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import falx_gb300 as fx
+    from falx_gb300 import _lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    host = make_input(args.size)
+    n = int(host.size)
+    pinned = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = host
+    data = pinned.to("cuda", non_blocking=False)
+
+    eng = fx.Engine(local)
+    schema = fx.Schema(fx.CSV_HASH, SCHEMA_COLS)
+    cs = schema.to_c()
+    stream = torch.cuda.current_stream()
+    eng.lib.falx_set_stream(eng.ctx, ctypes.c_void_p(stream.cuda_stream))
+
+    # Size outputs from a first pass.
+    idx_cap = n // 4 + 1024
+    rows_cap = n // 8 + 64
+    str_cap = n
+    index = torch.empty(idx_cap, dtype=torch.int32, device="cuda")
+    bufs = eng.alloc_columns(schema, rows_cap, str_cap)
+    cols = eng.columns_struct(schema, bufs, rows_cap, str_cap)
+    fb = _lib.falx_field_byte_stats()
+    out = _lib.falx_outputs()
+    out.index = index.data_ptr()
+    out.index_cap = idx_cap
+    out.columns = ctypes.pointer(cols)
+    out.field_bytes = ctypes.pointer(fb)
+
+    def step():
+        rc = eng.lib.falx_parse(eng.ctx, ctypes.byref(cs), ctypes.c_void_p(data.data_ptr()), n, ctypes.byref(out))
+        _lib.check(rc, "falx_parse")
+
+    step()
+    n_struct, rows = out.n_index, cols.rows
+    str_len = cols.cols[1].str_len
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    per = []
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ev0.record(stream)
+            step()
+            ev1.record(stream)
+            ev1.synchronize()
+            per.append(ev0.elapsed_time(ev1))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    ms = sum(per) / len(per)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * world / GIB / (ms / 1e3)
+
+    # Algorithmic bytes per launch: input + index + columns + validity + string offsets/arena.
+    words = (rows + 63) // 64
+    algo = n + 4 * n_struct + rows * (4 + 4 + 8 + 8) + 5 * words * 8 + 4 * (rows + 1) + str_len
+    peak, peak_kind = peaks()
+    achieved = algo / (ms / 1e3) / 1e9
+
+    # End to end through the host-buffer C ABI entry point.
+    h_index = np.empty(idx_cap, dtype=np.uint32)
+    h_vals = []
+    hcols = _lib.falx_columns()
+    hcols.rows_cap = rows_cap
+    for k, (f, t) in enumerate(SCHEMA_COLS):
+        if t == fx.STR:
+            v = np.empty(rows_cap + 1, dtype=np.int32)
+            sd = np.empty(str_cap, dtype=np.uint8)
+            hcols.cols[k].str_data = sd.ctypes.data
+            hcols.cols[k].str_cap = str_cap
+        else:
+            v = np.empty(rows_cap, dtype=np.float64 if t == fx.F64 else np.uint32)
+            sd = None
+        valid = np.empty((rows_cap + 63) // 64, dtype=np.uint64)
+        hcols.cols[k].values = v.ctypes.data
+        hcols.cols[k].valid = valid.ctypes.data
+        h_vals.append((v, valid, sd))
+    hfb = _lib.falx_field_byte_stats()
+    hout = _lib.falx_outputs()
+    hout.index = h_index.ctypes.data
+    hout.index_cap = idx_cap
+    hout.columns = ctypes.pointer(hcols)
+    hout.field_bytes = ctypes.pointer(hfb)
+    src = pinned.numpy()
+
+    def e2e_step():
+        rc = eng.lib.falx_parse_host(eng.ctx, ctypes.byref(cs), ctypes.c_void_p(src.ctypes.data), n,
+                                     ctypes.byref(hout))
+        _lib.check(rc, "falx_parse_host")
+
+    e2e_step()
+    e2e_t = []
+    for _ in range(max(2, min(args.steps, 5))):
+        s = time.perf_counter()
+        e2e_step()
+        e2e_t.append(time.perf_counter() - s)
+    e2e_s = sum(e2e_t) / len(e2e_t)
+    d2h = 4 * n_struct + rows * (4 + 4 + 8 + 8) + 5 * words * 8 + 4 * (rows + 1) + str_len
+    e2e = {"value": round(n / GIB / e2e_s, 4), "unit": "GiB/s", "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, sb = cpu_baseline(args.cpu_sample, threads)
+        cpu = {"value": round(v, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
+               "sample": "%d-byte csv_hash document: parallel index + field bytes + columns" % sb}
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "GiB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "csv_hash 1 GiB device-resident: structural index + field bytes + typed columns "
+                               "(u32 id, str City, u32 population, f64 lat, f64 lon)",
+                   "bytes": n, "structurals": int(n_struct), "rows": int(rows), "tile_bytes": 16384,
+                   "l2": "input 1 GiB > L2, no flush", "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes": int(algo)},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "field_bytes": {"fields": fb.fields, "bytes": fb.bytes},
+        "wall_s": round(wall, 3),
+    }
+    print(json.dumps(line))
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="falx_gb300")
+    ap.add_argument("--size", type=int, default=1 << 30)
+    ap.add_argument("--cpu-sample", type=int, default=64 << 20)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,119 @@
+"""ctypes view of include/falx_gpu.h. Loading fails loudly if the engine
+library is missing: there is no CPU fallback."""
+
+import ctypes
+import os
+from ctypes import POINTER, Structure, c_char_p, c_double, c_int, c_int32, c_int64, c_uint32, c_uint64, c_void_p
+
+from . import build
+
+FALX_OK = 0
+FALX_ERR_INVALID = -1
+FALX_ERR_CAPACITY = -2
+FALX_ERR_INPUT_TOO_LARGE = -3
+FALX_ERR_SCHEMA = -4
+FALX_ERR_TIMEOUT = -5
+FALX_ERR_CUDA = -6
+FALX_ERR_OVERFLOW = -7
+
+CSV, CSV_HASH, TSV, LOGFMT, NDJSON = 0, 1, 2, 3, 4
+I64, U32, F64, STR, BYTES = 0, 1, 2, 3, 4
+MAX_COLUMNS = 32
+
+
+class falx_column(Structure):
+    _fields_ = [("field", c_uint32), ("type", c_uint32)]
+
+
+class falx_schema(Structure):
+    _fields_ = [("dialect", c_int32), ("ncols", c_uint32), ("cols", falx_column * MAX_COLUMNS)]
+
+
+class falx_column_out(Structure):
+    _fields_ = [("values", c_void_p), ("valid", c_void_p), ("str_data", c_void_p), ("str_cap", c_uint64),
+                ("str_len", c_uint64)]
+
+
+class falx_columns(Structure):
+    _fields_ = [("rows_cap", c_uint64), ("rows", c_uint64), ("cols", falx_column_out * MAX_COLUMNS)]
+
+
+class falx_geo_stats(Structure):
+    _fields_ = [("records", c_uint64), ("values", c_uint64 * 2), ("checksum", c_uint64 * 2),
+                ("sum_e6", c_int64 * 2), ("inexact", c_uint64 * 2), ("sum_f64", c_double * 2)]
+
+
+class falx_field_byte_stats(Structure):
+    _fields_ = [("fields", c_uint64), ("bytes", c_uint64)]
+
+
+class falx_outputs(Structure):
+    _fields_ = [("index", c_void_p), ("index_cap", c_uint64), ("n_index", c_uint64),
+                ("seps", c_void_p), ("seps_cap", c_uint64), ("n_seps", c_uint64),
+                ("ends", c_void_p), ("ends_cap", c_uint64), ("n_ends", c_uint64),
+                ("columns", POINTER(falx_columns)), ("field_bytes", POINTER(falx_field_byte_stats)),
+                ("stats", POINTER(falx_geo_stats)), ("stats_fields", c_uint32 * 2)]
+
+
+class falx_ndjson_stats(Structure):
+    _fields_ = [("records", c_uint64), ("sum_id", c_int64), ("sum_score_e6", c_int64),
+                ("total_e6_lo", c_int64), ("total_e6_hi", c_int64), ("total_f64", c_double)]
+
+
+# Every symbol the header declares, with its signature.
+SIGNATURES = {
+    "falx_create": (c_int, [c_int, POINTER(c_void_p)]),
+    "falx_destroy": (None, [c_void_p]),
+    "falx_set_stream": (c_int, [c_void_p, c_void_p]),
+    "falx_strerror": (c_char_p, [c_int]),
+    "falx_index_structurals": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64)]),
+    "falx_parse_tape": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, c_void_p, c_uint64,
+                                POINTER(c_uint64), POINTER(c_uint64)]),
+    "falx_parse_columns": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, POINTER(falx_columns)]),
+    "falx_stats_count_sum": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_uint32, c_uint32,
+                                     POINTER(falx_geo_stats)]),
+    "falx_field_bytes": (c_int, [c_void_p, c_int, c_void_p, c_uint64, POINTER(falx_field_byte_stats)]),
+    "falx_parse": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, POINTER(falx_outputs)]),
+    "falx_ndjson_id_score": (c_int, [c_void_p, c_void_p, c_uint64, POINTER(falx_ndjson_stats)]),
+    "falx_index_structurals_host": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64,
+                                            POINTER(c_uint64)]),
+    "falx_parse_host": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, POINTER(falx_outputs)]),
+}
+
+_lib = None
+
+
+def lib_path():
+    return build.GPU_LIB
+
+
+def load(build_if_missing=True):
+    """Load the engine library (building it in-tree if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("falx_gb300: CUDA engine library %s is missing (run falx_gb300.build)" % path)
+        build.build_gpu()
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class FalxError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        msg = load().falx_strerror(code).decode()
+        super().__init__("%s failed: %s (%d)" % (what, msg, code))
+
+
+def check(code, what):
+    if code != FALX_OK:
+        raise FalxError(code, what)
+    return code

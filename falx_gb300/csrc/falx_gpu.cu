@@ -1,0 +1,944 @@
+// GB300 engine for the falx structural-index / column-materialisation path.
+//
+// One persistent kernel per call. CTAs take 16 KiB tiles from an atomic
+// ticket counter, stage each tile (plus a few bytes before it and, when rows
+// are materialised, a halo after it) into shared memory with a TMA bulk copy
+// that is issued one tile ahead, classify bytes with 4-byte SWAR tests, scan
+// the dialect's region automaton as packed transfer functions (thread ->
+// warp -> block), and chain tiles with a bounded decoupled look-back: first
+// the region state (so every tile resolves quotes / comments / escapes
+// without a second read of the input), then the output offsets. Positions
+// are compacted with popc ranks through shared memory and written coalesced.
+//
+// Reference mapping (Mapika/falx):
+//   step() + prefix_xor + push_indexes    csv_geo.rs:2117-2170, csv_hash.rs:2125-2222,
+//                                          tsv.rs:1302-1308, logfmt.rs:994-1012, ndjson.rs:1017-1033
+//   three-phase region scan (csv_hash)    csv_hash.rs:152-214, :345-399, :1921-1955
+//   speculative quote parity (csv)        csv_geo.rs:95-149
+//   tape (parse / records / fields)       csv_geo.rs:394-686, :1838-1849
+//   ColumnSink / stats / field bytes      csv_geo.rs:952-1101, :1491-1770; csv_hash.rs:965-1435
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "../../include/falx_gpu.h"
+#include "ndjson.cuh"
+#include "rows.cuh"
+#include "scan_core.cuh"
+
+namespace falx {
+
+constexpr uint64_t kWaitNs = 4000000000ull;  // every device-side wait gives up after 4 s
+
+struct TileStatus {   // 48 bytes, one per tile; every field is written once per launch
+    uint32_t flag;    // epoch * 4 + level (1: function, 2: exit state + counts, 3: + inclusive)
+    uint32_t func;    // transfer function (valid from level 1)
+    uint32_t exit;    // exit region state (valid from level 2)
+    uint32_t agg[3];  // structurals, terminators, rows in the tile (level 2)
+    uint32_t incl[3]; // inclusive prefix of agg (level 3)
+    uint32_t pad[3];
+};
+
+struct ArenaStatus {  // 48 bytes: prefix of string-arena bytes for up to kMaxStr columns
+    uint32_t flag;    // epoch * 4 + level (1: aggregate, 2: inclusive)
+    uint32_t pad[3];
+    uint32_t agg[kMaxStr];
+    uint32_t incl[kMaxStr];
+};
+
+struct DevHeader {
+    uint32_t ticket;
+    uint32_t abort;
+    uint32_t error;
+    uint32_t pad;
+    unsigned long long n_struct, n_terms, n_rows;
+    unsigned long long arena[kMaxStr];
+    unsigned long long fb_fields, fb_bytes;
+    unsigned long long st_records, st_values[2], st_checksum[2], st_sum_e6[2], st_inexact[2];
+};
+
+enum : uint32_t { ERR_TIMEOUT = 1, ERR_ARENA = 2, ERR_TMA = 4 };
+
+struct Params {
+    const uint8_t *data;
+    const uint8_t *abase;  // data rounded down to 16 bytes
+    uint64_t len;
+    uint32_t shift;        // data - abase
+    uint32_t num_tiles;
+    uint32_t epoch;
+    uint32_t halo;         // halo bytes staged after each tile (rows only)
+    TileStatus *status;
+    ArenaStatus *astatus;
+    DevHeader *hdr;
+    uint32_t *index;
+    uint64_t index_cap;
+    uint32_t *seps;
+    uint64_t seps_cap;
+    uint64_t *ends;
+    uint64_t ends_cap;
+    RowSpec rows;
+};
+
+// Shared-memory layout (dynamic).
+template <bool ROWS>
+struct Smem {
+    static constexpr int kHalo = ROWS ? kHaloBytes : 0;
+    static constexpr int kBuf = kPre + kTile + kHalo;  // multiple of 16
+    alignas(128) uint8_t buf[2][kBuf];
+    uint16_t stage[kTile + kHalo];
+    uint64_t bar[2];
+    uint32_t tile_of[2];
+    uint32_t warp_f[kWarps];
+    unsigned long long warp_c[kWarps];
+    uint32_t entry_state;
+    uint32_t tile_f;
+    uint32_t base[3];       // global structural / terminator / row offsets of the tile
+    unsigned long long tile_c;
+    RowShared<ROWS> rs;
+};
+
+__device__ __forceinline__ bool aborted(const DevHeader *h) {
+    return *(volatile const uint32_t *)&h->abort != 0;
+}
+
+__device__ __forceinline__ void fail(DevHeader *h, uint32_t bits) {
+    atomicOr(&h->error, bits);
+    atomicExch(&h->abort, 1u);
+}
+
+// Issue the bulk copy of tile `t` into `dst` (thread 0 only).
+template <bool ROWS>
+__device__ __forceinline__ void issue_tile(const Params &p, uint32_t t, uint8_t *dst, uint64_t *bar) {
+    constexpr int kBuf = Smem<ROWS>::kBuf;
+    const uint8_t *lo_full = p.abase + (uint64_t)t * kTile - kPre;  // address of dst[0]
+    const uint8_t *lo = t == 0 ? p.abase : lo_full;
+    const uint8_t *end16 = p.abase + ((p.shift + p.len + 15) & ~15ull);
+    const uint8_t *hi = lo_full + kBuf;
+    if (hi > end16) hi = end16;
+    uint32_t bytes = (uint32_t)(hi - lo);
+    mbar_expect_tx(bar, bytes);
+    bulk_g2s(dst + (lo - lo_full), lo, bytes, bar);
+}
+
+// Inclusive warp scan of transfer functions.
+__device__ __forceinline__ uint32_t warp_scan_f(uint32_t f, int lane) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t o = __shfl_up_sync(0xffffffffu, f, d);
+        if (lane >= d) f = fcompose(o, f);
+    }
+    return f;
+}
+
+__device__ __forceinline__ unsigned long long warp_scan_sum(unsigned long long v, int lane) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        unsigned long long o = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += o;
+    }
+    return v;
+}
+
+// Count fields packed 21 bits apart: structurals | terminators << 21 | rows << 42.
+__device__ __forceinline__ uint32_t cfield(unsigned long long c, int k) {
+    return (uint32_t)((c >> (21 * k)) & 0x1FFFFFull);
+}
+
+// Look-back for the tile's entry region state (thread 0).
+__device__ uint32_t lookback_state(const Params &p, uint32_t tile) {
+    uint32_t acc = kIdentity;  // composition of the functions of tiles j+1 .. tile-1
+    for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
+        const uint32_t *fp = &p.status[j].flag;
+        uint32_t flag = 0;
+        uint32_t polls = 0;
+        const uint64_t t0 = globaltimer_ns();
+        for (;;) {
+            flag = ld_acquire(fp);
+            if ((flag >> 2) == p.epoch && (flag & 3) >= 1) break;
+            if ((++polls & 255) == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs)) {
+                fail(p.hdr, ERR_TIMEOUT);
+                return 0;
+            }
+            __nanosleep(64);
+        }
+        if ((flag & 3) >= 2) return fapply(acc, ld_relaxed(&p.status[j].exit));
+        acc = fcompose(ld_relaxed(&p.status[j].func), acc);
+        if (j == 0) return fapply(acc, 0);
+    }
+    return 0;  // tile 0 starts outside every region
+}
+
+// Look-back for the tile's output offsets (thread 0).
+__device__ void lookback_counts(const Params &p, uint32_t tile, uint32_t out[3]) {
+    uint32_t s0 = 0, s1 = 0, s2 = 0;
+    for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
+        const uint32_t *fp = &p.status[j].flag;
+        uint32_t flag = 0;
+        uint32_t polls = 0;
+        const uint64_t t0 = globaltimer_ns();
+        for (;;) {
+            flag = ld_acquire(fp);
+            if ((flag >> 2) == p.epoch && (flag & 3) >= 2) break;
+            if ((++polls & 255) == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs)) {
+                fail(p.hdr, ERR_TIMEOUT);
+                out[0] = out[1] = out[2] = 0;
+                return;
+            }
+            __nanosleep(64);
+        }
+        if ((flag & 3) == 3) {
+            s0 += ld_relaxed(&p.status[j].incl[0]);
+            s1 += ld_relaxed(&p.status[j].incl[1]);
+            s2 += ld_relaxed(&p.status[j].incl[2]);
+            break;
+        }
+        s0 += ld_relaxed(&p.status[j].agg[0]);
+        s1 += ld_relaxed(&p.status[j].agg[1]);
+        s2 += ld_relaxed(&p.status[j].agg[2]);
+    }
+    out[0] = s0; out[1] = s1; out[2] = s2;
+}
+
+template <int D, bool ROWS>
+__device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uint32_t tile, uint8_t *b) {
+    constexpr int kBuf = Smem<ROWS>::kBuf;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t vs = (int64_t)tile * kTile - (int64_t)p.shift;  // file position of b[kPre]
+    const int64_t len = (int64_t)p.len;
+
+    // Bytes outside the file read as zero (the reference zero-pads its tail).
+    if (vs - kPre < 0 || vs - kPre + kBuf > len) {
+        for (int i = tid; i < kBuf; i += kThreads) {
+            int64_t v = vs - kPre + i;
+            if (v < 0 || v >= len) b[i] = 0;
+        }
+        __syncthreads();
+    }
+
+    // ---- classify this thread's 64 bytes (rotated chunks: conflict-free LDS.128)
+    const int r = (lane >> 1) & 3;
+    uint32_t w[16];
+    const uint4 *src = reinterpret_cast<const uint4 *>(b + kPre + tid * kThreadBytes);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        uint4 v = src[(k + r) & 3];
+        w[4 * k] = v.x; w[4 * k + 1] = v.y; w[4 * k + 2] = v.z; w[4 * k + 3] = v.w;
+    }
+    const Masks m = classify<D>(w, r);
+    const int64_t base_t = vs + (int64_t)tid * kThreadBytes;
+    const bool prev_nl = b[kPre + tid * kThreadBytes - 1] == '\n';
+    uint64_t ls = (m.nl << 1) | (uint64_t)prev_nl;
+    if (base_t <= 0 && base_t + kThreadBytes > 0) ls |= 1ull << (-base_t);
+
+    // ---- transfer functions: thread -> warp -> block
+    const uint32_t f = thread_function<D>(m, ls);
+    uint32_t incl = warp_scan_f(f, lane);
+    if (lane == 31) S.warp_f[warp] = incl;
+    uint32_t excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = kIdentity;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t wf = lane < kWarps ? S.warp_f[lane] : kIdentity;
+        uint32_t wi = warp_scan_f(wf, lane);
+        uint32_t we = __shfl_up_sync(0xffffffffu, wi, 1);
+        if (lane == 0) we = kIdentity;
+        if (lane < kWarps) S.warp_f[lane] = we;
+        if (lane == kWarps - 1) S.tile_f = wi;
+    }
+    __syncthreads();
+    excl = fcompose(S.warp_f[warp], excl);
+
+    // ---- publish the tile's function, look back for its entry state
+    if (tid == 0) {
+        TileStatus *st = &p.status[tile];
+        st->func = S.tile_f;
+        st_release(&st->flag, p.epoch * 4 + 1);
+        S.entry_state = lookback_state(p, tile);
+    }
+    __syncthreads();
+    const uint32_t entry = S.entry_state;
+    const uint32_t s_in = fapply(excl, entry);
+
+    // ---- structural, terminator and record-start masks
+    const uint64_t stm = structural_mask<D>(m, ls, s_in);
+    const uint64_t term = stm & m.nl;
+    uint64_t rows_m = 0;
+    if (ROWS) {
+        uint64_t rs = (term << 1) | (uint64_t)(prev_nl && state_outside<D>(s_in));
+        if (base_t <= 0 && base_t + kThreadBytes > 0) rs |= 1ull << (-base_t);
+        // Only starts inside the file own a record.
+        int64_t live = len - base_t;
+        if (live < kThreadBytes) rs &= live <= 0 ? 0 : ((1ull << live) - 1);
+        if (base_t < 0) rs &= ~((1ull << (-base_t)) - 1);
+        // csv_hash: a record whose first byte is '#' is a comment, not a row.
+        if (D == D_CSV_HASH) rs &= ~(m.x);
+        rows_m = rs;
+    }
+    const unsigned long long c = (unsigned long long)__popcll(stm) | ((unsigned long long)__popcll(term) << 21) |
+                                 ((unsigned long long)__popcll(rows_m) << 42);
+    unsigned long long ci = warp_scan_sum(c, lane);
+    if (lane == 31) S.warp_c[warp] = ci;
+    unsigned long long ce = ci - c;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long wc = lane < kWarps ? S.warp_c[lane] : 0ull;
+        unsigned long long wi = warp_scan_sum(wc, lane);
+        if (lane < kWarps) S.warp_c[lane] = wi - wc;
+        if (lane == kWarps - 1) S.tile_c = wi;
+    }
+    __syncthreads();
+    ce += S.warp_c[warp];
+
+    // ---- publish exit state + counts; look back for output offsets
+    if (tid == 0) {
+        TileStatus *st = &p.status[tile];
+        const unsigned long long tc = S.tile_c;
+        uint32_t a0 = cfield(tc, 0), a1 = cfield(tc, 1), a2 = cfield(tc, 2);
+        st->exit = fapply(S.tile_f, entry);
+        st->agg[0] = a0; st->agg[1] = a1; st->agg[2] = a2;
+        st_release(&st->flag, p.epoch * 4 + 2);
+        uint32_t pre[3];
+        lookback_counts(p, tile, pre);
+        st->incl[0] = pre[0] + a0; st->incl[1] = pre[1] + a1; st->incl[2] = pre[2] + a2;
+        st_release(&st->flag, p.epoch * 4 + 3);
+        S.base[0] = pre[0]; S.base[1] = pre[1]; S.base[2] = pre[2];
+        if (tile == p.num_tiles - 1) {
+            p.hdr->n_struct = pre[0] + a0;
+            p.hdr->n_terms = pre[1] + a1;
+            p.hdr->n_rows = pre[2] + a2;
+        }
+    }
+
+    // ---- stage positions (tile-relative, bit 15 = terminator) in rank order
+    {
+        uint32_t k = cfield(ce, 0);
+        uint64_t mm = stm;
+        while (mm) {
+            unsigned bpos = __ffsll((long long)mm) - 1;
+            uint32_t rel = (uint32_t)(tid * kThreadBytes + bpos);
+            S.stage[k++] = (uint16_t)(rel | (((term >> bpos) & 1) << 15));
+            mm &= mm - 1;
+        }
+    }
+    __syncthreads();
+    const uint32_t n_tile = cfield(S.tile_c, 0);
+    const uint32_t sbase = S.base[0];
+
+    // ---- structural index, coalesced
+    if (p.index) {
+        for (uint32_t i = tid; i < n_tile; i += kThreads) {
+            uint64_t g = (uint64_t)sbase + i;
+            if (g < p.index_cap) p.index[g] = (uint32_t)(vs + (S.stage[i] & 0x7FFF));
+        }
+    }
+    // ---- tape: separators and record ends
+    if (p.seps || p.ends) {
+        const uint32_t tbase = S.base[1];
+        const uint32_t my_s = cfield(ce, 0), my_t = cfield(ce, 1);
+        uint64_t sep_before = (uint64_t)(sbase - tbase) + (my_s - my_t);  // separators before this thread
+        uint64_t term_before = (uint64_t)tbase + my_t;
+        uint64_t mm = stm;
+        while (mm) {
+            unsigned bpos = __ffsll((long long)mm) - 1;
+            uint64_t pos = (uint64_t)(base_t + bpos);
+            if ((term >> bpos) & 1) {
+                if (p.ends && term_before < p.ends_cap) p.ends[term_before] = (sep_before << 32) | pos;
+                term_before++;
+            } else {
+                if (p.seps && sep_before < p.seps_cap) p.seps[sep_before] = (uint32_t)pos;
+                sep_before++;
+            }
+            mm &= mm - 1;
+        }
+    }
+
+    if constexpr (ROWS) {
+        RowCtx rc;
+        rc.vs = vs;
+        rc.len = len;
+        rc.buf = b;
+        rc.buf_end = vs - kPre + kBuf;
+        rc.n_tile = n_tile;
+        rc.row_base = S.base[2];
+        rc.exit_state = fapply(S.tile_f, entry);
+        rc.tile = tile;
+        rc.epoch = p.epoch;
+        rc.data = p.data;
+        rc.astatus = reinterpret_cast<void *>(p.astatus);
+        rc.hdr_arena = p.hdr->arena;
+        rc.hdr_fb = &p.hdr->fb_fields;
+        rc.hdr_st = &p.hdr->st_records;
+        rc.hdr_error = &p.hdr->error;
+        rc.hdr_abort = &p.hdr->abort;
+        rc.last_tile = tile == p.num_tiles - 1;
+        rows_phase<D>(p.rows, rc, S.rs, S.stage, rows_m, stm, term, cfield(ce, 0), cfield(ce, 2), base_t, tid);
+    }
+}
+
+template <int D, bool ROWS>
+__global__ void __launch_bounds__(kThreads) scan_kernel(const Params p) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    Smem<ROWS> &S = *reinterpret_cast<Smem<ROWS> *>(smem_raw);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        fence_mbar_init();
+        for (int s = 0; s < 2; s++) {
+            uint32_t t = atomicAdd(&p.hdr->ticket, 1u);
+            S.tile_of[s] = t;
+            if (t < p.num_tiles) issue_tile<ROWS>(p, t, S.buf[s], &S.bar[s]);
+        }
+    }
+    __syncthreads();
+    uint32_t phase[2] = {0, 0};
+    int s = 0;
+    for (;;) {
+        const uint32_t tile = S.tile_of[s];
+        if (tile >= p.num_tiles) break;
+        const bool ok = mbar_wait(&S.bar[s], phase[s], kWaitNs);
+        // One decision for the whole CTA: a timed-out copy or an abort stops it.
+        if (__syncthreads_or(!ok || (tid == 0 && aborted(p.hdr)))) {
+            if (tid == 0 && !ok) fail(p.hdr, ERR_TMA);
+            break;
+        }
+        phase[s] ^= 1;
+        process_tile<D, ROWS>(p, S, tile, S.buf[s]);
+        __syncthreads();  // every read of buf[s] and S.* for this tile is done
+        if (tid == 0) {
+            uint32_t t = atomicAdd(&p.hdr->ticket, 1u);
+            S.tile_of[s] = t;
+            if (t < p.num_tiles) {
+                fence_proxy_async();
+                issue_tile<ROWS>(p, t, S.buf[s], &S.bar[s]);
+            }
+        }
+        __syncthreads();
+        s ^= 1;
+    }
+    // Drain a bulk copy still in flight so the CTA never exits under it.
+    if (tid == 0) {
+        for (int k = 0; k < 2; k++) {
+            int sl = s ^ k;
+            if (S.tile_of[sl] < p.num_tiles && sl != s) mbar_wait(&S.bar[sl], phase[sl], kWaitNs);
+        }
+    }
+}
+
+}  // namespace falx
+
+// ===========================================================================
+// Host side.
+// ===========================================================================
+using namespace falx;
+
+struct falx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    int blocks_per_sm[5][2] = {};
+    TileStatus *status = nullptr;
+    ArenaStatus *astatus = nullptr;
+    uint32_t status_cap = 0;
+    uint32_t epoch = 0;
+    DevHeader *hdr = nullptr;   // device
+    DevHeader *hhdr = nullptr;  // pinned host mirror
+    // staging for the host-buffer entry points
+    uint8_t *dev_in = nullptr;
+    uint64_t dev_in_cap = 0;
+    void *dev_out = nullptr;
+    uint64_t dev_out_cap = 0;
+    NdjsonAcc *nd_acc = nullptr;   // device
+    NdjsonAcc *nd_host = nullptr;  // pinned
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e) {
+    if (e == cudaSuccess) return FALX_OK;
+    (void)cudaGetLastError();
+    return FALX_ERR_CUDA;
+}
+#define FALX_CUDA(x)                         \
+    do {                                     \
+        cudaError_t e_ = (x);                \
+        if (e_ != cudaSuccess) return cuda_fail(e_); \
+    } while (0)
+
+template <int D, bool ROWS>
+int setup_kernel(falx_ctx *c) {
+    size_t smem = sizeof(Smem<ROWS>);
+    FALX_CUDA(cudaFuncSetAttribute(scan_kernel<D, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nb = 0;
+    FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<D, ROWS>, kThreads, smem));
+    c->blocks_per_sm[D][ROWS] = nb > 0 ? nb : 1;
+    return FALX_OK;
+}
+
+int ensure_status(falx_ctx *c, uint32_t tiles) {
+    if (tiles <= c->status_cap && c->epoch < (1u << 28)) {
+        c->epoch++;
+        return FALX_OK;
+    }
+    if (tiles > c->status_cap) {
+        if (c->status) cudaFree(c->status);
+        if (c->astatus) cudaFree(c->astatus);
+        c->status = nullptr;
+        c->astatus = nullptr;
+        uint32_t cap = tiles < 1024 ? 1024 : tiles + tiles / 4;
+        FALX_CUDA(cudaMalloc(&c->status, sizeof(TileStatus) * (size_t)cap));
+        FALX_CUDA(cudaMalloc(&c->astatus, sizeof(ArenaStatus) * (size_t)cap));
+        c->status_cap = cap;
+    }
+    FALX_CUDA(cudaMemsetAsync(c->status, 0, sizeof(TileStatus) * (size_t)c->status_cap, c->stream));
+    FALX_CUDA(cudaMemsetAsync(c->astatus, 0, sizeof(ArenaStatus) * (size_t)c->status_cap, c->stream));
+    c->epoch = 1;
+    return FALX_OK;
+}
+
+bool valid_dialect(int d) { return d >= FALX_CSV && d <= FALX_NDJSON; }
+
+// Launch the scan over [data, data+len) with the outputs in `P` (device).
+int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t len, Params P) {
+    uint64_t shift = (uint64_t)((uintptr_t)data & 15u);
+    uint64_t tiles64 = (len + shift + kTile - 1) / kTile;
+    uint32_t tiles = (uint32_t)tiles64;
+    int rc = ensure_status(c, tiles);
+    if (rc) return rc;
+    FALX_CUDA(cudaMemsetAsync(c->hdr, 0, sizeof(DevHeader), c->stream));
+    P.data = data;
+    P.abase = data - shift;
+    P.len = len;
+    P.shift = (uint32_t)shift;
+    P.num_tiles = tiles;
+    P.epoch = c->epoch;
+    P.status = c->status;
+    P.astatus = c->astatus;
+    P.hdr = c->hdr;
+    P.halo = rows ? kHaloBytes : 0;
+    int nb = c->blocks_per_sm[dialect][rows ? 1 : 0];
+    uint64_t grid = (uint64_t)c->sm_count * (uint64_t)nb;
+    if (grid > tiles) grid = tiles;
+    if (grid == 0) grid = 1;
+#define FALX_LAUNCH(D)                                                                          \
+    do {                                                                                        \
+        if (rows)                                                                               \
+            scan_kernel<D, true><<<(unsigned)grid, kThreads, sizeof(Smem<true>), c->stream>>>(P);  \
+        else                                                                                    \
+            scan_kernel<D, false><<<(unsigned)grid, kThreads, sizeof(Smem<false>), c->stream>>>(P); \
+    } while (0)
+    switch (dialect) {
+    case FALX_CSV: FALX_LAUNCH(D_CSV); break;
+    case FALX_CSV_HASH: FALX_LAUNCH(D_CSV_HASH); break;
+    case FALX_TSV: FALX_LAUNCH(D_TSV); break;
+    case FALX_LOGFMT: FALX_LAUNCH(D_LOGFMT); break;
+    default: FALX_LAUNCH(D_NDJSON); break;
+    }
+#undef FALX_LAUNCH
+    FALX_CUDA(cudaGetLastError());
+    FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->hhdr->error & ERR_TIMEOUT) return FALX_ERR_TIMEOUT;
+    if (c->hhdr->error & ERR_TMA) return FALX_ERR_TIMEOUT;
+    if (c->hhdr->error & ERR_ARENA) return FALX_ERR_OVERFLOW;
+    return FALX_OK;
+}
+
+int check_common(falx_ctx *c, int dialect, const void *data, uint64_t len) {
+    if (!c || !valid_dialect(dialect)) return FALX_ERR_INVALID;
+    if (len && !data) return FALX_ERR_INVALID;
+    if (len >= (1ull << 32)) return FALX_ERR_INPUT_TOO_LARGE;
+    return FALX_OK;
+}
+
+int validate_schema(const falx_schema *s, RowSpec &rs, uint64_t rows_cap, const falx_columns *cols) {
+    if (s->ncols > FALX_MAX_COLUMNS) return FALX_ERR_INVALID;
+    rs.ncols = (int)s->ncols;
+    int nstr = 0;
+    rs.max_field = 0;
+    for (uint32_t k = 0; k < s->ncols; k++) {
+        uint32_t ty = s->cols[k].type;
+        if (ty > FALX_BYTES) return FALX_ERR_INVALID;
+        rs.field[k] = s->cols[k].field;
+        rs.type[k] = ty;
+        if (s->cols[k].field + 1 > rs.max_field) rs.max_field = s->cols[k].field + 1;
+        rs.str_slot[k] = -1;
+        if (ty == FALX_STR) {
+            if (nstr >= kMaxStr) return FALX_ERR_INVALID;
+            rs.str_slot[k] = nstr++;
+        }
+        if (cols) {
+            const falx_column_out &o = cols->cols[k];
+            if (rows_cap && (!o.values || !o.valid)) return FALX_ERR_INVALID;
+            if (ty == FALX_STR && o.str_cap && !o.str_data) return FALX_ERR_INVALID;
+            rs.values[k] = o.values;
+            rs.valid[k] = o.valid;
+            rs.str_data[k] = o.str_data;
+            rs.str_cap[k] = o.str_cap;
+        }
+    }
+    rs.nstr = nstr;
+    rs.rows_cap = rows_cap;
+    return FALX_OK;
+}
+
+int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, uint64_t len, falx_outputs *o) {
+    if (!schema || !o) return FALX_ERR_INVALID;
+    int dialect = schema->dialect;
+    int rc = check_common(c, dialect, data, len);
+    if (rc) return rc;
+    if (dialect == FALX_NDJSON && (o->columns || o->field_bytes || o->stats)) return FALX_ERR_INVALID;
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.index = o->index_cap ? o->index : nullptr;
+    P.index_cap = o->index_cap;
+    P.seps = o->seps_cap ? o->seps : nullptr;
+    P.seps_cap = o->seps_cap;
+    P.ends = o->ends_cap ? o->ends : nullptr;
+    P.ends_cap = o->ends_cap;
+    if ((o->index_cap && !o->index) || (o->seps_cap && !o->seps) || (o->ends_cap && !o->ends))
+        return FALX_ERR_INVALID;
+    bool rows = o->columns || o->field_bytes || o->stats;
+    RowSpec &rs = P.rows;
+    rs.ncols = 0;
+    rs.nstr = 0;
+    rs.max_field = 0;
+    rs.rows_cap = 0;
+    if (o->columns) {
+        rc = validate_schema(schema, rs, o->columns->rows_cap, o->columns);
+        if (rc) return rc;
+        for (int k = 0; k < rs.ncols; k++) {
+            uint64_t words = (o->columns->rows_cap + 63) / 64;
+            if (words) FALX_CUDA(cudaMemsetAsync(rs.valid[k], 0, words * 8, c->stream));
+        }
+    }
+    rs.want_fb = o->field_bytes != nullptr;
+    rs.want_stats = o->stats != nullptr;
+    rs.stats_field[0] = o->stats_fields[0];
+    rs.stats_field[1] = o->stats_fields[1];
+    if (rs.want_stats) {
+        uint32_t mf = (o->stats_fields[0] > o->stats_fields[1] ? o->stats_fields[0] : o->stats_fields[1]) + 1;
+        if (mf > rs.max_field) rs.max_field = mf;
+    }
+    o->n_index = o->n_seps = o->n_ends = 0;
+    if (o->columns) o->columns->rows = 0;
+    if (len == 0) {
+        if (o->columns) {
+            for (int k = 0; k < rs.ncols; k++) {
+                o->columns->cols[k].str_len = 0;
+                if (rs.type[k] == FALX_STR && o->columns->rows_cap + 1 > 0 && rs.values[k])
+                    FALX_CUDA(cudaMemsetAsync(rs.values[k], 0, 4, c->stream));
+            }
+            FALX_CUDA(cudaStreamSynchronize(c->stream));
+        }
+        if (o->field_bytes) o->field_bytes->fields = o->field_bytes->bytes = 0;
+        if (o->stats) memset(o->stats, 0, sizeof *o->stats);
+        return FALX_OK;
+    }
+    rc = run_scan(c, dialect, rows, data, len, P);
+    if (rc) return rc;
+    const DevHeader &h = *c->hhdr;
+    o->n_index = h.n_struct;
+    o->n_ends = h.n_terms;
+    o->n_seps = h.n_struct - h.n_terms;
+    bool cap_err = (o->index_cap && h.n_struct > o->index_cap) || (o->ends_cap && o->n_ends > o->ends_cap) ||
+                   (o->seps_cap && o->n_seps > o->seps_cap);
+    if (o->columns) {
+        o->columns->rows = h.n_rows;
+        if (h.n_rows > o->columns->rows_cap) cap_err = true;
+        for (int k = 0; k < rs.ncols; k++) {
+            if (rs.str_slot[k] >= 0) {
+                o->columns->cols[k].str_len = h.arena[rs.str_slot[k]];
+                if (h.arena[rs.str_slot[k]] > o->columns->cols[k].str_cap) cap_err = true;
+            } else {
+                o->columns->cols[k].str_len = 0;
+            }
+        }
+    }
+    if (o->field_bytes) {
+        o->field_bytes->fields = h.fb_fields;
+        o->field_bytes->bytes = h.fb_bytes;
+    }
+    if (o->stats) {
+        falx_geo_stats &s = *o->stats;
+        s.records = h.st_records;
+        for (int k = 0; k < 2; k++) {
+            s.values[k] = h.st_values[k];
+            s.checksum[k] = h.st_checksum[k];
+            s.sum_e6[k] = (int64_t)h.st_sum_e6[k];
+            s.inexact[k] = h.st_inexact[k];
+            s.sum_f64[k] = (double)(int64_t)h.st_sum_e6[k] / 1e6;
+        }
+    }
+    return cap_err ? FALX_ERR_CAPACITY : FALX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *falx_strerror(int code) {
+    switch (code) {
+    case FALX_OK: return "ok";
+    case FALX_ERR_INVALID: return "invalid argument";
+    case FALX_ERR_CAPACITY: return "output capacity too small";
+    case FALX_ERR_INPUT_TOO_LARGE: return "input must be shorter than 4 GiB";
+    case FALX_ERR_SCHEMA: return "record outside the expected schema";
+    case FALX_ERR_TIMEOUT: return "device-side wait gave up";
+    case FALX_ERR_CUDA: return "CUDA runtime error";
+    case FALX_ERR_OVERFLOW: return "string arena exceeds 2 GiB";
+    default: return "unknown error";
+    }
+}
+
+int falx_create(int device, falx_ctx **out) {
+    if (!out) return FALX_ERR_INVALID;
+    *out = nullptr;
+    FALX_CUDA(cudaSetDevice(device));
+    falx_ctx *c = new (std::nothrow) falx_ctx;
+    if (!c) return FALX_ERR_INVALID;
+    c->device = device;
+    int rc = FALX_OK;
+    if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) rc = FALX_ERR_CUDA;
+#define FALX_SETUP(D)                                  \
+    if (!rc) rc = setup_kernel<D, false>(c);           \
+    if (!rc) rc = setup_kernel<D, true>(c);
+    FALX_SETUP(D_CSV) FALX_SETUP(D_CSV_HASH) FALX_SETUP(D_TSV) FALX_SETUP(D_LOGFMT) FALX_SETUP(D_NDJSON)
+#undef FALX_SETUP
+    if (!rc && cudaMalloc(&c->hdr, sizeof(DevHeader)) != cudaSuccess) rc = FALX_ERR_CUDA;
+    if (!rc && cudaMallocHost(&c->hhdr, sizeof(DevHeader)) != cudaSuccess) rc = FALX_ERR_CUDA;
+    if (!rc) rc = ndjson_setup(c->device);
+    if (!rc && cudaMalloc(&c->nd_acc, sizeof(NdjsonAcc)) != cudaSuccess) rc = FALX_ERR_CUDA;
+    if (!rc && cudaMallocHost(&c->nd_host, sizeof(NdjsonAcc)) != cudaSuccess) rc = FALX_ERR_CUDA;
+    if (rc) {
+        falx_destroy(c);
+        (void)cudaGetLastError();
+        return rc;
+    }
+    *out = c;
+    return FALX_OK;
+}
+
+void falx_destroy(falx_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->status) cudaFree(c->status);
+    if (c->astatus) cudaFree(c->astatus);
+    if (c->hdr) cudaFree(c->hdr);
+    if (c->hhdr) cudaFreeHost(c->hhdr);
+    if (c->dev_in) cudaFree(c->dev_in);
+    if (c->dev_out) cudaFree(c->dev_out);
+    if (c->nd_acc) cudaFree(c->nd_acc);
+    if (c->nd_host) cudaFreeHost(c->nd_host);
+    delete c;
+}
+
+int falx_set_stream(falx_ctx *c, void *stream) {
+    if (!c) return FALX_ERR_INVALID;
+    c->stream = (cudaStream_t)stream;
+    return FALX_OK;
+}
+
+int falx_index_structurals(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, uint32_t *out,
+                           uint64_t cap, uint64_t *n_out) {
+    if (!n_out) return FALX_ERR_INVALID;
+    falx_schema s;
+    memset(&s, 0, sizeof s);
+    s.dialect = dialect;
+    falx_outputs o;
+    memset(&o, 0, sizeof o);
+    o.index = out;
+    o.index_cap = cap;
+    int rc = parse_device(c, &s, data, len, &o);
+    *n_out = o.n_index;
+    if (!rc && !cap && o.n_index) rc = FALX_ERR_CAPACITY;
+    return rc;
+}
+
+int falx_parse_tape(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, uint32_t *seps,
+                    uint64_t seps_cap, uint64_t *ends, uint64_t ends_cap, uint64_t *n_seps, uint64_t *n_ends) {
+    if (!n_seps || !n_ends) return FALX_ERR_INVALID;
+    falx_schema s;
+    memset(&s, 0, sizeof s);
+    s.dialect = dialect;
+    falx_outputs o;
+    memset(&o, 0, sizeof o);
+    o.seps = seps;
+    o.seps_cap = seps_cap;
+    o.ends = ends;
+    o.ends_cap = ends_cap;
+    // Counts come from the structural scan even when a capacity is zero.
+    int rc = parse_device(c, &s, data, len, &o);
+    *n_seps = o.n_seps;
+    *n_ends = o.n_ends;
+    if (!rc && ((!seps_cap && o.n_seps) || (!ends_cap && o.n_ends))) rc = FALX_ERR_CAPACITY;
+    return rc;
+}
+
+int falx_parse_columns(falx_ctx *c, const falx_schema *schema, const uint8_t *data, uint64_t len,
+                       falx_columns *out) {
+    if (!schema || !out) return FALX_ERR_INVALID;
+    falx_outputs o;
+    memset(&o, 0, sizeof o);
+    o.columns = out;
+    return parse_device(c, schema, data, len, &o);
+}
+
+int falx_stats_count_sum(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, uint32_t field0,
+                         uint32_t field1, falx_geo_stats *out) {
+    if (!out) return FALX_ERR_INVALID;
+    falx_schema s;
+    memset(&s, 0, sizeof s);
+    s.dialect = dialect;
+    falx_outputs o;
+    memset(&o, 0, sizeof o);
+    o.stats = out;
+    o.stats_fields[0] = field0;
+    o.stats_fields[1] = field1;
+    return parse_device(c, &s, data, len, &o);
+}
+
+int falx_field_bytes(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, falx_field_byte_stats *out) {
+    if (!out) return FALX_ERR_INVALID;
+    falx_schema s;
+    memset(&s, 0, sizeof s);
+    s.dialect = dialect;
+    falx_outputs o;
+    memset(&o, 0, sizeof o);
+    o.field_bytes = out;
+    return parse_device(c, &s, data, len, &o);
+}
+
+int falx_parse(falx_ctx *c, const falx_schema *schema, const uint8_t *data, uint64_t len, falx_outputs *out) {
+    return parse_device(c, schema, data, len, out);
+}
+
+int falx_ndjson_id_score(falx_ctx *c, const uint8_t *data, uint64_t len, falx_ndjson_stats *out) {
+    if (!c || !out) return FALX_ERR_INVALID;
+    if (len && !data) return FALX_ERR_INVALID;
+    if (len >= (1ull << 32)) return FALX_ERR_INPUT_TOO_LARGE;
+    FALX_CUDA(cudaSetDevice(c->device));
+    return ndjson_run(data, len, out, c->nd_acc, c->nd_host, c->stream);
+}
+
+static int grow(void **p, uint64_t *cap, uint64_t need) {
+    if (need <= *cap) return FALX_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    uint64_t n = need + need / 8 + 4096;
+    FALX_CUDA(cudaMalloc(p, n));
+    *cap = n;
+    return FALX_OK;
+}
+
+int falx_index_structurals_host(falx_ctx *c, int dialect, const uint8_t *host_data, uint64_t len,
+                                uint32_t *host_out, uint64_t cap, uint64_t *n_out) {
+    if (!c || !n_out || (len && !host_data) || (cap && !host_out)) return FALX_ERR_INVALID;
+    FALX_CUDA(cudaSetDevice(c->device));
+    int rc = grow((void **)&c->dev_in, &c->dev_in_cap, len);
+    if (rc) return rc;
+    rc = grow(&c->dev_out, &c->dev_out_cap, cap * 4);
+    if (rc) return rc;
+    if (len) FALX_CUDA(cudaMemcpyAsync(c->dev_in, host_data, len, cudaMemcpyHostToDevice, c->stream));
+    rc = falx_index_structurals(c, dialect, c->dev_in, len, (uint32_t *)c->dev_out, cap, n_out);
+    if (rc && rc != FALX_ERR_CAPACITY) return rc;
+    uint64_t n = *n_out < cap ? *n_out : cap;
+    if (n) FALX_CUDA(cudaMemcpyAsync(host_out, c->dev_out, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    return rc;
+}
+
+// Host-buffer form of falx_parse: `host_out` holds HOST pointers (index,
+// seps, ends, column buffers); they are staged through device buffers that
+// the context owns and reuses across calls.
+int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_data, uint64_t len,
+                    falx_outputs *host_out) {
+    if (!c || !schema || !host_out || (len && !host_data)) return FALX_ERR_INVALID;
+    FALX_CUDA(cudaSetDevice(c->device));
+    const falx_columns *hc = host_out->columns;
+    // Device layout: [index][seps][ends][per column: values | valid | str]
+    uint64_t need = 0;
+    auto take = [&](uint64_t bytes) {
+        uint64_t at = (need + 255) & ~255ull;
+        need = at + bytes;
+        return at;
+    };
+    uint64_t o_index = take(host_out->index_cap * 4), o_seps = take(host_out->seps_cap * 4),
+             o_ends = take(host_out->ends_cap * 8);
+    uint64_t o_vals[FALX_MAX_COLUMNS], o_valid[FALX_MAX_COLUMNS], o_str[FALX_MAX_COLUMNS];
+    uint64_t vbytes[FALX_MAX_COLUMNS];
+    if (hc) {
+        if (schema->ncols > FALX_MAX_COLUMNS) return FALX_ERR_INVALID;
+        for (uint32_t k = 0; k < schema->ncols; k++) {
+            uint32_t ty = schema->cols[k].type;
+            uint64_t rc_ = hc->rows_cap;
+            vbytes[k] = ty == FALX_I64 || ty == FALX_F64 ? rc_ * 8 : ty == FALX_U32 ? rc_ * 4
+                        : ty == FALX_BYTES ? rc_ * 8 : (rc_ + 1) * 4;
+            o_vals[k] = take(vbytes[k]);
+            o_valid[k] = take((rc_ + 63) / 64 * 8);
+            o_str[k] = take(ty == FALX_STR ? hc->cols[k].str_cap : 0);
+        }
+    }
+    int rc = grow((void **)&c->dev_in, &c->dev_in_cap, len);
+    if (rc) return rc;
+    rc = grow(&c->dev_out, &c->dev_out_cap, need);
+    if (rc) return rc;
+    uint8_t *dout = (uint8_t *)c->dev_out;
+    if (len) FALX_CUDA(cudaMemcpyAsync(c->dev_in, host_data, len, cudaMemcpyHostToDevice, c->stream));
+    falx_outputs d = *host_out;
+    falx_columns dc;
+    if (host_out->index_cap) d.index = (uint32_t *)(dout + o_index);
+    if (host_out->seps_cap) d.seps = (uint32_t *)(dout + o_seps);
+    if (host_out->ends_cap) d.ends = (uint64_t *)(dout + o_ends);
+    if (hc) {
+        dc = *hc;
+        for (uint32_t k = 0; k < schema->ncols; k++) {
+            dc.cols[k].values = dout + o_vals[k];
+            dc.cols[k].valid = (uint64_t *)(dout + o_valid[k]);
+            dc.cols[k].str_data = schema->cols[k].type == FALX_STR ? dout + o_str[k] : nullptr;
+        }
+        d.columns = &dc;
+    }
+    rc = parse_device(c, schema, c->dev_in, len, &d);
+    if (rc && rc != FALX_ERR_CAPACITY) return rc;
+    auto back = [&](void *dst, const void *src, uint64_t bytes) -> int {
+        if (bytes && dst) FALX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+        return FALX_OK;
+    };
+    int r2 = FALX_OK;
+    uint64_t ni = d.n_index < host_out->index_cap ? d.n_index : host_out->index_cap;
+    uint64_t ns = d.n_seps < host_out->seps_cap ? d.n_seps : host_out->seps_cap;
+    uint64_t ne = d.n_ends < host_out->ends_cap ? d.n_ends : host_out->ends_cap;
+    if (!r2) r2 = back(host_out->index, d.index, ni * 4);
+    if (!r2) r2 = back(host_out->seps, d.seps, ns * 4);
+    if (!r2) r2 = back(host_out->ends, d.ends, ne * 8);
+    if (hc) {
+        falx_columns *ho = host_out->columns;
+        uint64_t rows = dc.rows < hc->rows_cap ? dc.rows : hc->rows_cap;
+        for (uint32_t k = 0; k < schema->ncols && !r2; k++) {
+            uint32_t ty = schema->cols[k].type;
+            uint64_t vb = ty == FALX_I64 || ty == FALX_F64 || ty == FALX_BYTES ? rows * 8
+                          : ty == FALX_U32 ? rows * 4 : (rows + 1) * 4;
+            r2 = back(ho->cols[k].values, dc.cols[k].values, vb);
+            if (!r2) r2 = back(ho->cols[k].valid, dc.cols[k].valid, (rows + 63) / 64 * 8);
+            if (!r2 && ty == FALX_STR) {
+                uint64_t sl = dc.cols[k].str_len < hc->cols[k].str_cap ? dc.cols[k].str_len : hc->cols[k].str_cap;
+                r2 = back(ho->cols[k].str_data, dc.cols[k].str_data, sl);
+            }
+            ho->cols[k].str_len = dc.cols[k].str_len;
+        }
+        ho->rows = dc.rows;
+    }
+    if (!r2) FALX_CUDA(cudaStreamSynchronize(c->stream));
+    host_out->n_index = d.n_index;
+    host_out->n_seps = d.n_seps;
+    host_out->n_ends = d.n_ends;
+    return r2 ? r2 : rc;
+}
+
+}  // extern "C"

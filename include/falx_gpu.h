@@ -1,0 +1,187 @@
+/*
+ * falx_gpu.h — C ABI of the GB300 structural-index / column-materialisation
+ * engine. Drop-in boundary for the generated falx parser modules
+ * (Mapika/falx src/kernels/{csv_geo,csv_hash,csv_typed,tsv,logfmt,ndjson}.rs):
+ * each entry point below cites the reference function it replaces.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only. Unless a name says `_host`, data and
+ *    output buffers are device pointers in the context's device, owned by the
+ *    caller; the library never frees them.
+ *  - Every call is stream-ordered on the context's stream and returns after
+ *    the stream has drained, so counts are valid on return.
+ *  - Return 0 (FALX_OK) or a negative FALX_ERR_* code; nothing traps.
+ *    On FALX_ERR_CAPACITY the counts are still reported, so callers can
+ *    resize and retry (the reference's Vec outputs grow instead).
+ *  - Offsets are u32, so inputs must be shorter than 4 GiB
+ *    (the reference's limit as well: csv_geo.rs push_indexes stores u32).
+ *  - A context is single-stream and not thread-safe; use one per host thread.
+ */
+#ifndef FALX_GPU_H
+#define FALX_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FALX_OK 0
+#define FALX_ERR_INVALID (-1)          /* null pointer, unknown dialect, bad schema */
+#define FALX_ERR_CAPACITY (-2)         /* an output buffer is too small; counts reported */
+#define FALX_ERR_INPUT_TOO_LARGE (-3)  /* len >= 4 GiB */
+#define FALX_ERR_SCHEMA (-4)           /* NDJSON record outside the id+score schema */
+#define FALX_ERR_TIMEOUT (-5)          /* a device-side wait gave up; outputs undefined */
+#define FALX_ERR_CUDA (-6)             /* CUDA runtime error */
+#define FALX_ERR_OVERFLOW (-7)         /* string arena beyond i32 offsets (2 GiB) */
+
+/* Dialects (formats.rs:56-185). */
+typedef enum {
+    FALX_CSV = 0,      /* ',' '\n', doubled-quote regions          (csv_dialect) */
+    FALX_CSV_HASH = 1, /* as CSV plus '#' comment lines             (csv_hash_dialect) */
+    FALX_TSV = 2,      /* '\t' '\n', no quoting                     (tsv_dialect) */
+    FALX_LOGFMT = 3,   /* ' ' '=' '\n', backslash-escaped quotes    (logfmt_dialect) */
+    FALX_NDJSON = 4    /* '\n' outside backslash-escaped strings    (ndjson_dialect) */
+} falx_dialect;
+
+/* Column types (codegen.rs:78-93 ColumnType, plus U32). */
+typedef enum {
+    FALX_I64 = 0,   /* str::parse::<i64> */
+    FALX_U32 = 1,   /* str::parse::<u32> */
+    FALX_F64 = 2,   /* str::parse::<f64>, bit-exact */
+    FALX_STR = 3,   /* cleaned bytes, Arrow varbinary (i32 offsets + arena) */
+    FALX_BYTES = 4  /* raw (from,to) span, valid iff present and non-empty */
+} falx_col_type;
+
+#define FALX_MAX_COLUMNS 32 /* codegen.rs:198-205 */
+
+typedef struct falx_ctx falx_ctx;
+
+/* Context: device, stream, look-back scratch, tuned launch parameters. */
+int falx_create(int device, falx_ctx **out);
+void falx_destroy(falx_ctx *ctx);
+/* Use `stream` (a cudaStream_t; NULL = the legacy default stream). */
+int falx_set_stream(falx_ctx *ctx, void *stream);
+const char *falx_strerror(int code);
+
+/* Structural index: offsets of every structural byte, byte-identical to the
+ * serial path. Replaces index_structurals / index_structurals_par
+ * (csv_geo.rs:24, :95; csv_hash.rs:345; tsv.rs:20, :64; logfmt.rs;
+ * ndjson.rs). Writes min(n, cap) entries; *n_out = n. */
+int falx_index_structurals(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len,
+                           uint32_t *out, uint64_t cap, uint64_t *n_out);
+
+/* Tape behind parse() / parse_par() (csv_geo.rs:394, :215, push_tape
+ * :1838-1849): separator offsets, and per terminated record an end entry
+ * `(separators_before << 32) | terminator_offset`. Records / fields views
+ * are built on these two arrays by the host API. */
+int falx_parse_tape(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len,
+                    uint32_t *seps, uint64_t seps_cap, uint64_t *ends, uint64_t ends_cap,
+                    uint64_t *n_seps, uint64_t *n_ends);
+
+typedef struct {
+    uint32_t field; /* 0-based field ordinal within the record */
+    uint32_t type;  /* falx_col_type */
+} falx_column;
+
+typedef struct {
+    int32_t dialect;
+    uint32_t ncols;
+    falx_column cols[FALX_MAX_COLUMNS];
+} falx_schema;
+
+typedef struct {
+    void *values;      /* I64 int64[rows_cap]; U32 uint32[rows_cap]; F64 double[rows_cap];
+                          BYTES uint32[2*rows_cap] (from,to); STR int32 offsets[rows_cap+1] */
+    uint64_t *valid;   /* LSB-first validity bitmap, ceil(rows_cap/64) words */
+    uint8_t *str_data; /* STR arena */
+    uint64_t str_cap;
+    uint64_t str_len;  /* out: arena bytes used (STR) */
+} falx_column_out;
+
+typedef struct {
+    uint64_t rows_cap;
+    uint64_t rows; /* out */
+    falx_column_out cols[FALX_MAX_COLUMNS];
+} falx_columns;
+
+/* Typed columns (Arrow-compatible). Replaces parse_columns /
+ * parse_columns_par / parse_columns_chunks_par (csv_geo.rs:1112, :1216,
+ * :1167; csv_hash.rs:1451, :1570, :1507; csv_typed.rs). Comment records
+ * (csv_hash) are not rows. */
+int falx_parse_columns(falx_ctx *ctx, const falx_schema *schema, const uint8_t *data, uint64_t len,
+                       falx_columns *out);
+
+typedef struct {
+    uint64_t records;
+    uint64_t values[2];
+    uint64_t checksum[2]; /* wrapping sum of f64 bit patterns (csv_geo.rs:1735-1750) */
+    int64_t sum_e6[2];    /* exact sum of value*1e6 over cells exact in micro-units */
+    uint64_t inexact[2];  /* valid cells not exact in micro-units */
+    double sum_f64[2];    /* sum_e6 / 1e6 */
+} falx_geo_stats;
+
+/* Fused count / sum over two f64 fields without materialising columns.
+ * Replaces parse_csv_geo_stats / parse_csv_geo_stats_par
+ * (csv_geo.rs:1505, :1513). */
+int falx_stats_count_sum(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len, uint32_t field0,
+                         uint32_t field1, falx_geo_stats *out);
+
+typedef struct {
+    uint64_t fields;
+    uint64_t bytes;
+} falx_field_byte_stats;
+
+/* Field count and total cleaned field bytes. Replaces parse_field_bytes /
+ * parse_field_bytes_par (csv_hash.rs:976, :984). */
+int falx_field_bytes(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len,
+                     falx_field_byte_stats *out);
+
+/* Everything above from one pass over the input; NULL / zero-capacity
+ * members are skipped. The fused form of the entry points above. */
+typedef struct {
+    uint32_t *index;
+    uint64_t index_cap;
+    uint64_t n_index; /* out */
+    uint32_t *seps;
+    uint64_t seps_cap;
+    uint64_t n_seps; /* out */
+    uint64_t *ends;
+    uint64_t ends_cap;
+    uint64_t n_ends; /* out */
+    falx_columns *columns;
+    falx_field_byte_stats *field_bytes;
+    falx_geo_stats *stats;
+    uint32_t stats_fields[2];
+} falx_outputs;
+
+int falx_parse(falx_ctx *ctx, const falx_schema *schema, const uint8_t *data, uint64_t len,
+               falx_outputs *out);
+
+typedef struct {
+    uint64_t records;
+    int64_t sum_id;       /* wrapping */
+    int64_t sum_score_e6; /* wrapping */
+    int64_t total_e6_lo;  /* exact 128-bit sum of id*1e6 + score_e6 */
+    int64_t total_e6_hi;
+    double total_f64;     /* (double)total_e6 / 1e6 */
+} falx_ndjson_stats;
+
+/* sum(id + nested.score) over NDJSON records, JSON-aware (any key order,
+ * whitespace, escapes, decimal scores with up to 6 fraction digits). The
+ * generalisation of parse_ndjson_id_score(_par) (ndjson.rs:679, :726); a
+ * record outside the schema returns FALX_ERR_SCHEMA where the reference
+ * panics (ndjson.rs:721-724). */
+int falx_ndjson_id_score(falx_ctx *ctx, const uint8_t *data, uint64_t len, falx_ndjson_stats *out);
+
+/* Host-buffer forms for callers without device memory: copy `data` in,
+ * run, copy the results out, all on the context's stream. */
+int falx_index_structurals_host(falx_ctx *ctx, int dialect, const uint8_t *host_data, uint64_t len,
+                                uint32_t *host_out, uint64_t cap, uint64_t *n_out);
+int falx_parse_host(falx_ctx *ctx, const falx_schema *schema, const uint8_t *host_data, uint64_t len,
+                    falx_outputs *host_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,233 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the CPU oracle on
+seeded inputs, byte-for-byte / bit-for-bit."""
+
+import numpy as np
+import pytest
+
+import falx_gb300 as fx
+import oracle
+from conftest import DIALECT_ALPHABETS, Rng, random_doc
+from falx_gb300 import gen
+
+pytestmark = pytest.mark.gpu
+
+DIALECTS = [fx.CSV, fx.CSV_HASH, fx.TSV, fx.LOGFMT, fx.NDJSON]
+
+
+def gpu_index(engine, doc, dialect):
+    return engine.index_structurals(doc, dialect).cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("dialect", DIALECTS)
+def test_index_random_small(engine, dialect):
+    # Generated-kernel differential inputs (tests/codegen.rs:392-468).
+    rng = Rng(0xDEADBEEFCAFEBABE + dialect)
+    for _ in range(300):
+        doc = random_doc(rng, DIALECT_ALPHABETS[dialect], rng.next() % 300)
+        assert np.array_equal(gpu_index(engine, doc, dialect), oracle.index_spec(doc, dialect)), doc
+
+
+@pytest.mark.parametrize("dialect", DIALECTS)
+def test_index_random_long_and_misaligned(engine, dialect):
+    # 100 000-byte inputs (tests/codegen.rs:471-543) crossing many tiles,
+    # at every base-pointer alignment within 16 bytes.
+    rng = Rng(0xCAFEBABEDEADBEEF + dialect)
+    doc = random_doc(rng, DIALECT_ALPHABETS[dialect], 100_000)
+    big = engine.to_device(doc + b"\0" * 16)
+    for off in range(16):
+        sub = big[off: off + len(doc) - off]
+        want = oracle.index_spec(doc[off:], dialect)
+        assert np.array_equal(gpu_index(engine, sub, dialect), want), off
+
+
+@pytest.mark.parametrize("kind,dialect", [(gen.CSV_GEO, fx.CSV), (gen.CSV_HASH, fx.CSV_HASH), (gen.TSV, fx.TSV),
+                                          (gen.LOGFMT, fx.LOGFMT), (gen.NDJSON, fx.NDJSON),
+                                          (gen.ADVERSARIAL, fx.CSV_HASH)])
+def test_index_generated(engine, kind, dialect):
+    doc = gen.generate(kind, 6 << 20)
+    assert np.array_equal(gpu_index(engine, doc, dialect), oracle.index_spec(doc, dialect))
+
+
+@pytest.mark.parametrize("dialect", DIALECTS)
+def test_tape(engine, dialect):
+    doc = gen.generate({fx.CSV: gen.CSV_GEO, fx.CSV_HASH: gen.ADVERSARIAL, fx.TSV: gen.TSV, fx.LOGFMT: gen.LOGFMT,
+                        fx.NDJSON: gen.NDJSON}[dialect], 3 << 20)
+    seps, ends = engine.parse_tape(doc, dialect)
+    ws, we = oracle.parse_tape(doc, dialect)
+    assert np.array_equal(seps.cpu().numpy().view(np.uint32), ws)
+    assert np.array_equal(ends.cpu().numpy().view(np.uint64), we)
+
+
+@pytest.mark.parametrize("doc", [
+    b"", b",", b"\n", b"a", b"\r\n", b'"', b'"unterminated,\n,x', b",,,,\n\n\n", b"#", b"#x\n", b'#"\na,b\n',
+    b"," * 100_000, b"\n" * 100_000, b'"' * 99_999, b"x" * 70_000,
+])
+@pytest.mark.parametrize("dialect", DIALECTS)
+def test_index_edges(engine, doc, dialect):
+    assert np.array_equal(gpu_index(engine, doc, dialect), oracle.index_spec(doc, dialect))
+
+
+def compare_columns(got, rows, want, cols):
+    assert got.rows == rows
+    for k, (_, t) in enumerate(cols):
+        h = got.host(k)
+        assert np.array_equal(h["valid"], want[k]["valid"]), "validity, column %d" % k
+        if t == fx.STR:
+            assert np.array_equal(h["offsets"], want[k]["offsets"]), "offsets, column %d" % k
+            assert h["data"] == want[k]["data"], "arena, column %d" % k
+        elif t == fx.BYTES:
+            assert np.array_equal(h["spans"], want[k]["spans"]), "spans, column %d" % k
+        else:
+            assert np.array_equal(h["values"].view(np.uint8), np.asarray(want[k]["values"]).view(np.uint8)), \
+                "values, column %d" % k
+
+
+GEO_COLS = [(0, fx.U32), (1, fx.STR), (2, fx.STR), (3, fx.U32), (4, fx.F64), (5, fx.F64)]
+TYPED_COLS = [(0, fx.I64), (1, fx.STR), (2, fx.F64), (4, fx.BYTES)]
+
+
+@pytest.mark.parametrize("kind,dialect", [(gen.CSV_GEO, fx.CSV), (gen.CSV_HASH, fx.CSV_HASH), (gen.TSV, fx.TSV),
+                                          (gen.ADVERSARIAL, fx.CSV_HASH)])
+def test_columns_generated(engine, kind, dialect):
+    doc = gen.generate(kind, 4 << 20)
+    got = engine.parse_columns(doc, fx.Schema(dialect, GEO_COLS))
+    rows, want = oracle.parse_columns(doc, dialect, GEO_COLS)
+    compare_columns(got, rows, want, GEO_COLS)
+
+
+def typed_random_doc(rng):
+    # The cell mix of tests/columns.rs:454-620 (randomized_differential).
+    out = bytearray()
+    for _ in range(rng.next() % 40 + 1):
+        nf = rng.next() % 8
+        crlf = rng.next() % 10 < 1
+        for fi in range(nf):
+            if fi:
+                out += b","
+            ct = rng.next() % 7
+            if ct == 0:
+                sign = b"-" if rng.next() % 2 == 0 else b"+"
+                if rng.next() % 3 == 0:
+                    out += sign
+                out += bytes(48 + rng.next() % 10 for _ in range(rng.next() % 22 + 1))
+            elif ct == 1:
+                if rng.next() % 2 == 0:
+                    out += b"-"
+                st = rng.next() % 5
+                if st == 0:
+                    out += bytes(48 + rng.next() % 10 for _ in range(rng.next() % 18 + 1)) + b"."
+                    out += bytes(48 + rng.next() % 10 for _ in range(rng.next() % 18))
+                elif st == 1:
+                    out += bytes(48 + rng.next() % 10 for _ in range(rng.next() % 15 + 1))
+                elif st == 2:
+                    out += bytes(48 + rng.next() % 10 for _ in range(rng.next() % 8 + 1)) + b"e"
+                    if rng.next() % 2 == 0:
+                        out += b"-"
+                    e = (rng.next() % (1 << 32)) % 700 - 350
+                    out += str(abs(e)).encode()
+                elif st == 3:
+                    out += b"." + bytes(48 + rng.next() % 10 for _ in range(rng.next() % 15 + 1))
+                else:
+                    out += bytes(48 + rng.next() % 10 for _ in range(rng.next() % 15 + 1)) + b"."
+            elif ct == 2:
+                out += bytes(97 + rng.next() % 26 for _ in range(rng.next() % 10))
+            elif ct == 3:
+                pass
+            elif ct == 4:
+                out += [b"inf", b"nan", b"NaN"][rng.next() % 3]
+            else:
+                out += b'"'
+                for _ in range(rng.next() % 50):
+                    it = rng.next() % 5
+                    out += [b",", b'""', b"\n", b" ", bytes([97 + rng.next() % 26])][it]
+                out += b'"'
+        out += b"\r\n" if crlf else b"\n"
+    if rng.next() % 3 == 0:
+        for fi in range(rng.next() % 8):
+            if fi:
+                out += b","
+            out += bytes(48 + rng.next() % 10 for _ in range(rng.next() % 20))
+    return bytes(out)
+
+
+def test_columns_typed_random(engine):
+    rng = Rng(0xDEADBEEFCAFEBABE)
+    docs = [typed_random_doc(rng) for _ in range(200)]
+    for doc in docs:
+        got = engine.parse_columns(doc, fx.Schema(fx.CSV, TYPED_COLS))
+        rows, want = oracle.parse_columns(doc, fx.CSV, TYPED_COLS)
+        compare_columns(got, rows, want, TYPED_COLS)
+    big = b"".join(docs)
+    got = engine.parse_columns(big, fx.Schema(fx.CSV, TYPED_COLS))
+    rows, want = oracle.parse_columns(big, fx.CSV, TYPED_COLS)
+    compare_columns(got, rows, want, TYPED_COLS)
+
+
+def test_columns_long_records(engine):
+    # Records longer than the halo after a tile: quoted cells of 1-9 KiB.
+    rng = Rng(0x1234)
+    parts = []
+    for i in range(400):
+        n = 1000 + rng.next() % 8000 if i % 7 == 0 else rng.next() % 30
+        parts.append(b'%d,"%s",x,%d,%d.5,-1.25\n' % (i, b"a,\n#" * (n // 4), i, i))
+    doc = b"".join(parts)
+    for dialect in (fx.CSV, fx.CSV_HASH):
+        got = engine.parse_columns(doc, fx.Schema(dialect, GEO_COLS))
+        rows, want = oracle.parse_columns(doc, dialect, GEO_COLS)
+        compare_columns(got, rows, want, GEO_COLS)
+
+
+@pytest.mark.parametrize("doc", [b"", b"\n", b"a", b"a\r", b"\r\n", b"," * 100_000, b"\n" * 100_000,
+                                 b'"' * 99_999, b'1,"x\n', b"# c\n#d", b"1,2\n#\n3,4"])
+def test_columns_edges(engine, doc):
+    for dialect in (fx.CSV, fx.CSV_HASH):
+        got = engine.parse_columns(doc, fx.Schema(dialect, TYPED_COLS))
+        rows, want = oracle.parse_columns(doc, dialect, TYPED_COLS)
+        compare_columns(got, rows, want, TYPED_COLS)
+
+
+@pytest.mark.parametrize("kind,dialect", [(gen.CSV_HASH, fx.CSV_HASH), (gen.ADVERSARIAL, fx.CSV_HASH),
+                                          (gen.CSV_GEO, fx.CSV), (gen.TSV, fx.TSV)])
+def test_field_bytes(engine, kind, dialect):
+    doc = gen.generate(kind, 4 << 20)
+    fb = engine.field_bytes(doc, dialect)
+    assert (fb.fields, fb.bytes) == oracle.field_bytes(doc, dialect)
+
+
+@pytest.mark.parametrize("kind,dialect", [(gen.CSV_GEO, fx.CSV), (gen.CSV_HASH, fx.CSV_HASH)])
+def test_geo_stats(engine, kind, dialect):
+    doc = gen.generate(kind, 4 << 20)
+    st = engine.stats_count_sum(doc, dialect, 4, 5)
+    want = oracle.geo_stats(doc, dialect, 4, 5)
+    assert st.records == want.records
+    assert st.values == tuple(want.values)
+    assert st.checksum == tuple(want.checksum)
+    assert st.sum_e6 == tuple(want.sum_e6)
+    assert st.inexact == tuple(want.inexact)
+    for k in range(2):
+        # exact fixed point vs the reference's sequential f64 fold
+        assert abs(st.sum_f64[k] - want.fold[k]) <= 1e-12 * max(1.0, abs(want.fold[k])) + 1e-9
+
+
+def test_ndjson_known_answer(engine):
+    # tests/ndjson_id_score.rs:5-19: records=3, sum(id + score) = 62.
+    doc = (b'{"id":10,"name":"a","tags":["x","y"],"nested":{"score":7,"ok":true},"note":"plain"}\n'
+           b'{"id":-3,"name":"quoted \\" id\\":999","tags":["n","m"],"nested":{"score":11,"ok":true},'
+           b'"note":"brace } inside"}\n'
+           b'{"id":42,"name":"slash \\\\ nested score\\":123","tags":["p","q"],"nested":{"score":-5,"ok":true},'
+           b'"note":"end"}\n')
+    st = engine.ndjson_id_score(doc)
+    assert st.records == 3
+    assert st.total_e6 == 62 * 10**6
+    assert oracle.ndjson_literal(doc) == (3, 62)
+
+
+def test_ndjson_generated(engine):
+    doc = gen.generate(gen.NDJSON, 8 << 20)
+    st = engine.ndjson_id_score(doc)
+    want = oracle.ndjson_json(doc)
+    assert st.records == want["records"]
+    assert st.sum_id == want["sum_id"]
+    assert st.sum_score_e6 == want["sum_score_e6"]
+    assert st.total_e6 == want["total_e6"]
+    assert st.total_f64 == want["total_f64"]

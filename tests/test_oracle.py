@@ -1,0 +1,76 @@
+"""CPU checks of the oracle: the blockwise restatement of the generated step
+kernels against the byte-serial ground truth (the reference's own
+differential tests), and the cell decoders against Rust str::parse rules."""
+
+import math
+import struct
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import DIALECT_ALPHABETS, Rng, random_doc
+
+
+@pytest.mark.parametrize("dialect", [0, 1, 2, 3, 4])
+def test_blocks_match_spec_random(dialect):
+    # tests/codegen.rs:392-468: 800 random inputs per format, lengths < 300.
+    rng = Rng(0xDEADBEEFCAFEBABE + dialect)
+    for _ in range(800):
+        doc = random_doc(rng, DIALECT_ALPHABETS[dialect], rng.next() % 300)
+        assert np.array_equal(oracle.index_blocks(doc, dialect), oracle.index_spec(doc, dialect)), doc
+
+
+@pytest.mark.parametrize("dialect", [0, 1, 2, 3, 4])
+def test_blocks_match_spec_long(dialect):
+    # tests/codegen.rs:471-543: one 100 000-byte input per format.
+    rng = Rng(0xCAFEBABEDEADBEEF)
+    doc = random_doc(rng, DIALECT_ALPHABETS[dialect], 100_000)
+    assert np.array_equal(oracle.index_blocks(doc, dialect), oracle.index_spec(doc, dialect))
+
+
+def test_interp_matches_scalar_csv():
+    # src/lib.rs:48-67: 2000 random CSV inputs over `",\n\rxy`.
+    rng = Rng(0xD1B54A32D192ED03)
+    for _ in range(2000):
+        doc = random_doc(rng, b'",\n\rxy', rng.next() % 300)
+        assert np.array_equal(oracle.index_blocks(doc, 0), oracle.index_spec(doc, 0))
+
+
+def bits(x):
+    return struct.unpack("<Q", struct.pack("<d", x))[0]
+
+
+@pytest.mark.parametrize("cell,expect", [
+    (b"1.5", 1.5), (b"-0.0", -0.0), (b"0.1", 0.1), (b"1.5e308", 1.5e308), (b"5e-324", 5e-324),
+    (b"inf", math.inf), (b"-inf", -math.inf), (b"Infinity", math.inf), (b".5", 0.5), (b"5.", 5.0),
+    (b"+5", 5.0), (b"1e400", math.inf), (b"1e-400", 0.0), (b"-12.345678", -12.345678),
+    (b"1_000", None), (b"", None), (b"e5", None), (b"1e", None), (b".", None), (b" 1", None), (b"0x10", None),
+    (b"nan(1)", None), (b"+", None), (b"--1", None),
+])
+def test_parse_f64(cell, expect):
+    got = oracle.parse_f64(cell)
+    if expect is None:
+        assert got is None
+    else:
+        assert bits(got) == bits(expect)
+
+
+def test_parse_f64_nan_bits():
+    assert bits(oracle.parse_f64(b"NaN")) == 0x7FF8000000000000
+    assert bits(oracle.parse_f64(b"-nan")) == 0xFFF8000000000000
+
+
+@pytest.mark.parametrize("cell,expect", [
+    (b"9223372036854775807", 2**63 - 1), (b"-9223372036854775808", -2**63), (b"9223372036854775808", None),
+    (b"+5", 5), (b"-0", 0), (b"0007", 7), (b"", None), (b"+", None), (b"-", None), (b"1 ", None), (b"+-1", None),
+])
+def test_parse_i64(cell, expect):
+    assert oracle.parse_i64(cell) == expect
+
+
+@pytest.mark.parametrize("cell,expect", [
+    (b"4294967295", 4294967295), (b"4294967296", None), (b"+7", 7), (b"-0", None), (b"", None), (b"012", 12),
+])
+def test_parse_u32(cell, expect):
+    assert oracle.parse_u32(cell) == expect
