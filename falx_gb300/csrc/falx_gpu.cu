@@ -34,13 +34,18 @@ namespace falx {
 
 constexpr uint64_t kWaitNs = 4000000000ull;  // every device-side wait gives up after 4 s
 
-struct TileStatus {   // 48 bytes, one per tile; every field is written once per launch
-    uint32_t flag;    // epoch * 4 + level (1: function, 2: exit state + counts, 3: + inclusive)
-    uint32_t func;    // transfer function (valid from level 1)
-    uint32_t exit;    // exit region state (valid from level 2)
-    uint32_t agg[3];  // structurals, terminators, rows in the tile (level 2)
-    uint32_t incl[3]; // inclusive prefix of agg (level 3)
-    uint32_t pad[3];
+// One per tile. Level 1 publishes the tile's aggregate: its transfer function
+// and, for every possible entry state, its counts (structurals, terminators,
+// rows packed 21 bits apart). Level 2 publishes the inclusive prefix: the
+// absolute exit state and the counts of the whole file up to the tile end.
+// Every field is written once per launch, before the release of its level.
+struct TileStatus {      // 64 bytes
+    uint32_t flag;       // epoch * 4 + level
+    uint32_t func;       // transfer function (level 1)
+    uint64_t agg[4];     // packed counts per entry state (level 1)
+    uint32_t exit;       // exit state (level 2)
+    uint32_t incl[3];    // inclusive structurals, terminators, rows (level 2)
+    uint32_t pad[2];
 };
 
 struct ArenaStatus {  // 48 bytes: prefix of string-arena bytes for up to kMaxStr columns
@@ -83,6 +88,16 @@ struct Params {
     RowSpec rows;
 };
 
+// Shared state of the block-wide look-back.
+struct LookbackShared {
+    uint32_t wf[kWarps];
+    uint64_t wc[kWarps][4];
+    uint32_t nearest;
+    uint32_t stop;
+    uint32_t entry;
+    uint32_t pre[3];
+};
+
 // Shared-memory layout (dynamic).
 template <bool ROWS>
 struct Smem {
@@ -91,9 +106,10 @@ struct Smem {
     alignas(128) uint8_t buf[2][kBuf];
     uint16_t stage[kTile + kHalo];
     uint64_t bar[2];
-    uint32_t tile_of[2];
     uint32_t warp_f[kWarps];
     unsigned long long warp_c[kWarps];
+    unsigned long long warp_agg[kWarps][4];
+    LookbackShared lb;
     uint32_t entry_state;
     uint32_t tile_f;
     uint32_t base[3];       // global structural / terminator / row offsets of the tile
@@ -148,59 +164,166 @@ __device__ __forceinline__ uint32_t cfield(unsigned long long c, int k) {
     return (uint32_t)((c >> (21 * k)) & 0x1FFFFFull);
 }
 
-// Look-back for the tile's entry region state (thread 0).
-__device__ uint32_t lookback_state(const Params &p, uint32_t tile) {
-    uint32_t acc = kIdentity;  // composition of the functions of tiles j+1 .. tile-1
-    for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
-        const uint32_t *fp = &p.status[j].flag;
-        uint32_t flag = 0;
-        uint32_t polls = 0;
-        const uint64_t t0 = globaltimer_ns();
-        for (;;) {
-            flag = ld_acquire(fp);
-            if ((flag >> 2) == p.epoch && (flag & 3) >= 1) break;
-            if ((++polls & 255) == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs)) {
-                fail(p.hdr, ERR_TIMEOUT);
+// Number of region states of each dialect's automaton.
+template <int D>
+struct NStates {
+    static constexpr int value = D == D_TSV ? 1 : D == D_CSV ? 2 : D == D_CSV_HASH ? 3 : 4;
+};
+
+// Warp-wide spin until every lane's status word (lane l watches tile
+// hi - l) reaches `level` in this launch's epoch. Returns each lane's flag,
+// or sets `gave_up` after the wait bound or an abort.
+__device__ __forceinline__ uint32_t window_wait(const Params &p, int64_t hi, int lane, uint32_t level,
+                                                bool &gave_up) {
+    const int64_t j = hi - lane;
+    const bool in = j >= 0;
+    const uint64_t t0 = globaltimer_ns();
+    uint32_t flag = 0;
+    for (uint32_t it = 0;; it++) {
+        if (in) flag = ld_acquire(&p.status[j].flag);
+        bool ready = !in || ((flag >> 2) == p.epoch && (flag & 3) >= level);
+        if (__all_sync(0xffffffffu, ready)) break;
+        if ((it & 63) == 63) {
+            bool stop = lane == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
+            if (__any_sync(0xffffffffu, stop)) {
+                if (lane == 0) fail(p.hdr, ERR_TIMEOUT);
+                gave_up = true;
                 return 0;
             }
-            __nanosleep(64);
         }
-        if ((flag & 3) >= 2) return fapply(acc, ld_relaxed(&p.status[j].exit));
-        acc = fcompose(ld_relaxed(&p.status[j].func), acc);
-        if (j == 0) return fapply(acc, 0);
+        __nanosleep(32);
     }
-    return 0;  // tile 0 starts outside every region
+    return flag;
 }
 
-// Look-back for the tile's output offsets (thread 0).
-__device__ void lookback_counts(const Params &p, uint32_t tile, uint32_t out[3]) {
-    uint32_t s0 = 0, s1 = 0, s2 = 0;
-    for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
-        const uint32_t *fp = &p.status[j].flag;
-        uint32_t flag = 0;
-        uint32_t polls = 0;
-        const uint64_t t0 = globaltimer_ns();
-        for (;;) {
-            flag = ld_acquire(fp);
-            if ((flag >> 2) == p.epoch && (flag & 3) >= 2) break;
-            if ((++polls & 255) == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs)) {
-                fail(p.hdr, ERR_TIMEOUT);
-                out[0] = out[1] = out[2] = 0;
-                return;
-            }
-            __nanosleep(64);
-        }
-        if ((flag & 3) == 3) {
-            s0 += ld_relaxed(&p.status[j].incl[0]);
-            s1 += ld_relaxed(&p.status[j].incl[1]);
-            s2 += ld_relaxed(&p.status[j].incl[2]);
-            break;
-        }
-        s0 += ld_relaxed(&p.status[j].agg[0]);
-        s1 += ld_relaxed(&p.status[j].agg[1]);
-        s2 += ld_relaxed(&p.status[j].agg[2]);
+__device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Combine an older aggregate (gf, gc) into a newer one (f, c), in place:
+// (f . gf, gc[s] + c[gf(s)]).
+template <int NS>
+__device__ __forceinline__ void agg_prepend(uint32_t gf, const uint64_t (&gc)[4], uint32_t &f, uint64_t (&c)[4]) {
+    uint64_t r[4];
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+        const uint32_t m = fapply(gf, s);
+        uint64_t cm = c[0];
+#pragma unroll
+        for (int t = 1; t < NS; t++) cm = m == (uint32_t)t ? c[t] : cm;
+        r[s] = gc[s] + cm;
     }
-    out[0] = s0; out[1] = s1; out[2] = s2;
+#pragma unroll
+    for (int s = 0; s < NS; s++) c[s] = r[s];
+    f = fcompose(gf, f);
+}
+
+// Decoupled look-back over (transfer function, counts per entry state)
+// aggregates, run by one warp: lane l watches predecessor hi - l. A probe
+// ends as soon as every predecessor nearer than the nearest published
+// inclusive prefix has published its aggregate (it never waits on older
+// tiles than it needs); without an inclusive prefix in the window it needs the
+// whole window and moves 32 tiles further back. Combining an older segment A
+// with a newer B gives (f_B . f_A, c_A[s] + c_B[f_A(s)]). Returns the tile's
+// entry state and the counts of the file before the tile.
+template <int NS>
+__device__ uint32_t lookback(const Params &p, uint32_t tile, int lane, uint32_t pre[3]) {
+    uint32_t af = kIdentity;  // aggregate of the tiles between the window and `tile`
+    uint64_t ac[4] = {0, 0, 0, 0};
+    const uint64_t t0 = globaltimer_ns();
+    for (int64_t hi = (int64_t)tile - 1; hi >= 0; hi -= 32) {
+        const int64_t j = hi - lane;
+        const bool in = j >= 0;
+        uint32_t flag = 0, ball_incl = 0;
+        for (uint32_t it = 0;; it++) {
+            if (in) flag = ld_acquire(&p.status[j].flag);
+            const bool cur = (flag >> 2) == p.epoch;
+            const uint32_t not_ready = __ballot_sync(0xffffffffu, in && !(cur && (flag & 3) >= 1));
+            ball_incl = __ballot_sync(0xffffffffu, in && cur && (flag & 3) >= 2);
+            const int first_incl = ball_incl ? __ffs(ball_incl) - 1 : 32;
+            const int first_wait = not_ready ? __ffs(not_ready) - 1 : 32;
+            if (first_wait > first_incl || not_ready == 0) break;
+            if ((it & 63) == 63) {
+                const bool stop = lane == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
+                if (__any_sync(0xffffffffu, stop)) {
+                    if (lane == 0) fail(p.hdr, ERR_TIMEOUT);
+                    pre[0] = pre[1] = pre[2] = 0;
+                    return 0;
+                }
+            }
+            __nanosleep(32);
+        }
+        const int sidx = ball_incl ? __ffs(ball_incl) - 1 : 32;
+        uint32_t f = kIdentity;
+        uint64_t c[4] = {0, 0, 0, 0};
+        if (in && lane < sidx) {
+            f = ld_relaxed(&p.status[j].func);
+#pragma unroll
+            for (int s = 0; s < NS; s++) c[s] = ld_relaxed64(&p.status[j].agg[s]);
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t gf = __shfl_down_sync(0xffffffffu, f, d);
+            uint64_t gc[4];
+#pragma unroll
+            for (int s = 0; s < NS; s++) gc[s] = __shfl_down_sync(0xffffffffu, c[s], d);
+            if (lane + d < 32) agg_prepend<NS>(gf, gc, f, c);  // lane + d covers older tiles
+        }
+        uint32_t wf = __shfl_sync(0xffffffffu, f, 0);
+        uint64_t wc[4];
+#pragma unroll
+        for (int s = 0; s < NS; s++) wc[s] = __shfl_sync(0xffffffffu, c[s], 0);
+        agg_prepend<NS>(wf, wc, af, ac);
+        if (ball_incl) {
+            uint32_t ex = 0, i0 = 0, i1 = 0, i2 = 0;
+            if (lane == sidx) {
+                ex = ld_relaxed(&p.status[j].exit);
+                i0 = ld_relaxed(&p.status[j].incl[0]);
+                i1 = ld_relaxed(&p.status[j].incl[1]);
+                i2 = ld_relaxed(&p.status[j].incl[2]);
+            }
+            ex = __shfl_sync(0xffffffffu, ex, sidx);
+            uint64_t cc = ac[0];
+#pragma unroll
+            for (int t = 1; t < NS; t++) cc = ex == (uint32_t)t ? ac[t] : cc;
+            pre[0] = __shfl_sync(0xffffffffu, i0, sidx) + cfield(cc, 0);
+            pre[1] = __shfl_sync(0xffffffffu, i1, sidx) + cfield(cc, 1);
+            pre[2] = __shfl_sync(0xffffffffu, i2, sidx) + cfield(cc, 2);
+            return fapply(af, ex);
+        }
+    }
+    // reached the first tile: the file starts outside every region
+    pre[0] = cfield(ac[0], 0);
+    pre[1] = cfield(ac[0], 1);
+    pre[2] = cfield(ac[0], 2);
+    return fapply(af, 0);
+}
+
+// Record starts among this thread's 64 bytes for entry state s_in: file
+// position 0 and every byte after a structural newline, inside the file;
+// csv_hash records opening with '#' are comments, not rows.
+template <int D>
+__device__ __forceinline__ uint64_t row_starts(const Masks &m, uint64_t term, bool prev_nl, uint32_t s_in,
+                                               int64_t base_t, int64_t len) {
+    uint64_t rs = (term << 1) | (uint64_t)(prev_nl && state_outside<D>(s_in));
+    if (base_t <= 0 && base_t + kThreadBytes > 0) rs |= 1ull << (-base_t);
+    const int64_t live = len - base_t;
+    if (live < kThreadBytes) rs &= live <= 0 ? 0 : ((1ull << live) - 1);
+    if (base_t < 0) rs &= ~((1ull << (-base_t)) - 1);
+    if (D == D_CSV_HASH) rs &= ~(m.x);
+    return rs;
+}
+
+template <int D, bool ROWS>
+__device__ __forceinline__ unsigned long long thread_counts(const Masks &m, uint64_t ls, bool prev_nl, uint32_t s,
+                                                            int64_t base_t, int64_t len) {
+    const uint64_t st = structural_mask<D>(m, ls, s);
+    const uint64_t term = st & m.nl;
+    unsigned long long c = (unsigned long long)__popcll(st) | ((unsigned long long)__popcll(term) << 21);
+    if (ROWS) c |= (unsigned long long)__popcll(row_starts<D>(m, term, prev_nl, s, base_t, len)) << 42;
+    return c;
 }
 
 template <int D, bool ROWS>
@@ -252,34 +375,76 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uin
     __syncthreads();
     excl = fcompose(S.warp_f[warp], excl);
 
-    // ---- publish the tile's function, look back for its entry state
+    // ---- tile aggregate: function + counts for every entry state
+    constexpr int NS = NStates<D>::value;
+    unsigned long long cv[NS];
+#pragma unroll
+    for (int e = 0; e < NS; e++) cv[e] = thread_counts<D, ROWS>(m, ls, prev_nl, e, base_t, len);
+    {
+        unsigned long long v[NS];
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++) {
+            const uint32_t e = fapply(excl, s0);
+            unsigned long long x = cv[0];
+#pragma unroll
+            for (int t = 1; t < NS; t++) x = e == (uint32_t)t ? cv[t] : x;
+            v[s0] = x;
+        }
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++) {
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) v[s0] += __shfl_xor_sync(0xffffffffu, v[s0], d);
+            if (lane == 0) S.warp_agg[warp][s0] = v[s0];
+        }
+    }
+    __syncthreads();
+
+    // ---- publish the aggregate; one look-back gives entry state and offsets
+    unsigned long long agg[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int s0 = 0; s0 < NS; s0++)
+        for (int w2 = 0; w2 < kWarps; w2++) agg[s0] += S.warp_agg[w2][s0];
+    TileStatus *const tst = &p.status[tile];
     if (tid == 0) {
-        TileStatus *st = &p.status[tile];
-        st->func = S.tile_f;
-        st_release(&st->flag, p.epoch * 4 + 1);
-        S.entry_state = lookback_state(p, tile);
+        tst->func = S.tile_f;
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++) tst->agg[s0] = agg[s0];
+        st_release(&tst->flag, p.epoch * 4 + 1);
+    }
+    if (warp == 0) {
+        uint32_t pre[3];
+        const uint32_t e = lookback<NS>(p, tile, lane, pre);
+        if (lane == 0) {
+            unsigned long long mine = agg[0];
+#pragma unroll
+            for (int t = 1; t < NS; t++) mine = e == (uint32_t)t ? agg[t] : mine;
+            tst->exit = fapply(S.tile_f, e);
+            tst->incl[0] = pre[0] + cfield(mine, 0);
+            tst->incl[1] = pre[1] + cfield(mine, 1);
+            tst->incl[2] = pre[2] + cfield(mine, 2);
+            st_release(&tst->flag, p.epoch * 4 + 2);
+            S.entry_state = e;
+            S.base[0] = pre[0]; S.base[1] = pre[1]; S.base[2] = pre[2];
+            S.tile_c = mine;
+            if (tile == p.num_tiles - 1) {
+                p.hdr->n_struct = pre[0] + cfield(mine, 0);
+                p.hdr->n_terms = pre[1] + cfield(mine, 1);
+                p.hdr->n_rows = pre[2] + cfield(mine, 2);
+            }
+        }
     }
     __syncthreads();
     const uint32_t entry = S.entry_state;
     const uint32_t s_in = fapply(excl, entry);
 
-    // ---- structural, terminator and record-start masks
+    // ---- this thread's masks for its true entry state, ranks within the tile
     const uint64_t stm = structural_mask<D>(m, ls, s_in);
     const uint64_t term = stm & m.nl;
     uint64_t rows_m = 0;
-    if (ROWS) {
-        uint64_t rs = (term << 1) | (uint64_t)(prev_nl && state_outside<D>(s_in));
-        if (base_t <= 0 && base_t + kThreadBytes > 0) rs |= 1ull << (-base_t);
-        // Only starts inside the file own a record.
-        int64_t live = len - base_t;
-        if (live < kThreadBytes) rs &= live <= 0 ? 0 : ((1ull << live) - 1);
-        if (base_t < 0) rs &= ~((1ull << (-base_t)) - 1);
-        // csv_hash: a record whose first byte is '#' is a comment, not a row.
-        if (D == D_CSV_HASH) rs &= ~(m.x);
-        rows_m = rs;
-    }
-    const unsigned long long c = (unsigned long long)__popcll(stm) | ((unsigned long long)__popcll(term) << 21) |
-                                 ((unsigned long long)__popcll(rows_m) << 42);
+    if (ROWS) rows_m = row_starts<D>(m, term, prev_nl, s_in, base_t, len);
+    unsigned long long c = cv[0];
+#pragma unroll
+    for (int t = 1; t < NS; t++) c = s_in == (uint32_t)t ? cv[t] : c;
     unsigned long long ci = warp_scan_sum(c, lane);
     if (lane == 31) S.warp_c[warp] = ci;
     unsigned long long ce = ci - c;
@@ -288,30 +453,9 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uin
         unsigned long long wc = lane < kWarps ? S.warp_c[lane] : 0ull;
         unsigned long long wi = warp_scan_sum(wc, lane);
         if (lane < kWarps) S.warp_c[lane] = wi - wc;
-        if (lane == kWarps - 1) S.tile_c = wi;
     }
     __syncthreads();
     ce += S.warp_c[warp];
-
-    // ---- publish exit state + counts; look back for output offsets
-    if (tid == 0) {
-        TileStatus *st = &p.status[tile];
-        const unsigned long long tc = S.tile_c;
-        uint32_t a0 = cfield(tc, 0), a1 = cfield(tc, 1), a2 = cfield(tc, 2);
-        st->exit = fapply(S.tile_f, entry);
-        st->agg[0] = a0; st->agg[1] = a1; st->agg[2] = a2;
-        st_release(&st->flag, p.epoch * 4 + 2);
-        uint32_t pre[3];
-        lookback_counts(p, tile, pre);
-        st->incl[0] = pre[0] + a0; st->incl[1] = pre[1] + a1; st->incl[2] = pre[2] + a2;
-        st_release(&st->flag, p.epoch * 4 + 3);
-        S.base[0] = pre[0]; S.base[1] = pre[1]; S.base[2] = pre[2];
-        if (tile == p.num_tiles - 1) {
-            p.hdr->n_struct = pre[0] + a0;
-            p.hdr->n_terms = pre[1] + a1;
-            p.hdr->n_rows = pre[2] + a2;
-        }
-    }
 
     // ---- stage positions (tile-relative, bit 15 = terminator) in rank order
     {
@@ -375,57 +519,58 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uin
         rc.hdr_error = &p.hdr->error;
         rc.hdr_abort = &p.hdr->abort;
         rc.last_tile = tile == p.num_tiles - 1;
-        rows_phase<D>(p.rows, rc, S.rs, S.stage, rows_m, stm, term, cfield(ce, 0), cfield(ce, 2), base_t, tid);
+        // does the tile's first byte start a record (comment records included)?
+        const bool rec0 = vs <= 0 || (b[kPre - 1] == '\n' && state_outside<D>(entry));
+        rows_phase<D>(p.rows, rc, S.rs, S.stage, rows_m, stm, term, cfield(ce, 0), cfield(ce, 1), cfield(ce, 2),
+                      cfield(S.tile_c, 1), cfield(S.tile_c, 2), rec0, base_t, tid);
     }
 }
 
+// Persistent kernel, launched cooperatively so every CTA is resident. CTA c
+// takes tiles c, c + G, c + 2G, ... (G = grid size): each round of G
+// consecutive tiles is in flight at once and every look-back waits only on
+// tiles of the same or an earlier round, which resident CTAs are already
+// processing. The bulk copy of a CTA's next tile is issued one round ahead.
 template <int D, bool ROWS>
 __global__ void __launch_bounds__(kThreads) scan_kernel(const Params p) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     Smem<ROWS> &S = *reinterpret_cast<Smem<ROWS> *>(smem_raw);
     const int tid = threadIdx.x;
+    const uint32_t G = gridDim.x;
     if (tid == 0) {
         mbar_init(&S.bar[0], 1);
         mbar_init(&S.bar[1], 1);
         fence_mbar_init();
         for (int s = 0; s < 2; s++) {
-            uint32_t t = atomicAdd(&p.hdr->ticket, 1u);
-            S.tile_of[s] = t;
+            const uint32_t t = blockIdx.x + (uint32_t)s * G;
             if (t < p.num_tiles) issue_tile<ROWS>(p, t, S.buf[s], &S.bar[s]);
         }
     }
     __syncthreads();
     uint32_t phase[2] = {0, 0};
     int s = 0;
-    for (;;) {
-        const uint32_t tile = S.tile_of[s];
-        if (tile >= p.num_tiles) break;
+    for (uint32_t tile = blockIdx.x; tile < p.num_tiles; tile += G) {
         const bool ok = mbar_wait(&S.bar[s], phase[s], kWaitNs);
         // One decision for the whole CTA: a timed-out copy or an abort stops it.
         if (__syncthreads_or(!ok || (tid == 0 && aborted(p.hdr)))) {
-            if (tid == 0 && !ok) fail(p.hdr, ERR_TMA);
+            if (tid == 0) {
+                if (!ok) fail(p.hdr, ERR_TMA);
+                // never leave a bulk copy in flight into this CTA's shared memory
+                else if (tile + G < p.num_tiles) mbar_wait(&S.bar[s ^ 1], phase[s ^ 1], kWaitNs);
+            }
             break;
         }
         phase[s] ^= 1;
         process_tile<D, ROWS>(p, S, tile, S.buf[s]);
         __syncthreads();  // every read of buf[s] and S.* for this tile is done
         if (tid == 0) {
-            uint32_t t = atomicAdd(&p.hdr->ticket, 1u);
-            S.tile_of[s] = t;
+            const uint32_t t = tile + 2 * G;
             if (t < p.num_tiles) {
                 fence_proxy_async();
                 issue_tile<ROWS>(p, t, S.buf[s], &S.bar[s]);
             }
         }
-        __syncthreads();
         s ^= 1;
-    }
-    // Drain a bulk copy still in flight so the CTA never exits under it.
-    if (tid == 0) {
-        for (int k = 0; k < 2; k++) {
-            int sl = s ^ k;
-            if (S.tile_of[sl] < p.num_tiles && sl != s) mbar_wait(&S.bar[sl], phase[sl], kWaitNs);
-        }
     }
 }
 
@@ -441,6 +586,7 @@ struct falx_ctx {
     cudaStream_t stream = nullptr;
     int sm_count = 0;
     int blocks_per_sm[5][2] = {};
+    int ctas_per_sm = 0;  // FALX_CTAS_PER_SM caps the persistent grid (tuning)
     TileStatus *status = nullptr;
     ArenaStatus *astatus = nullptr;
     uint32_t status_cap = 0;
@@ -521,16 +667,21 @@ int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t 
     P.hdr = c->hdr;
     P.halo = rows ? kHaloBytes : 0;
     int nb = c->blocks_per_sm[dialect][rows ? 1 : 0];
+    if (c->ctas_per_sm > 0 && c->ctas_per_sm < nb) nb = c->ctas_per_sm;
     uint64_t grid = (uint64_t)c->sm_count * (uint64_t)nb;
     if (grid > tiles) grid = tiles;
     if (grid == 0) grid = 1;
-#define FALX_LAUNCH(D)                                                                          \
-    do {                                                                                        \
-        if (rows)                                                                               \
-            scan_kernel<D, true><<<(unsigned)grid, kThreads, sizeof(Smem<true>), c->stream>>>(P);  \
-        else                                                                                    \
-            scan_kernel<D, false><<<(unsigned)grid, kThreads, sizeof(Smem<false>), c->stream>>>(P); \
+#define FALX_LAUNCH(D)                                                                            \
+    do {                                                                                          \
+        void *args_[] = {(void *)&P};                                                             \
+        if (rows)                                                                                 \
+            err = cudaLaunchCooperativeKernel((const void *)scan_kernel<D, true>, dim3((unsigned)grid), \
+                                              dim3(kThreads), args_, sizeof(Smem<true>), c->stream);     \
+        else                                                                                      \
+            err = cudaLaunchCooperativeKernel((const void *)scan_kernel<D, false>, dim3((unsigned)grid), \
+                                              dim3(kThreads), args_, sizeof(Smem<false>), c->stream);    \
     } while (0)
+    cudaError_t err = cudaSuccess;
     switch (dialect) {
     case FALX_CSV: FALX_LAUNCH(D_CSV); break;
     case FALX_CSV_HASH: FALX_LAUNCH(D_CSV_HASH); break;
@@ -538,8 +689,8 @@ int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t 
     case FALX_LOGFMT: FALX_LAUNCH(D_LOGFMT); break;
     default: FALX_LAUNCH(D_NDJSON); break;
     }
+    FALX_CUDA(err);
 #undef FALX_LAUNCH
-    FALX_CUDA(cudaGetLastError());
     FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
     FALX_CUDA(cudaStreamSynchronize(c->stream));
     if (c->hhdr->error & ERR_TIMEOUT) return FALX_ERR_TIMEOUT;
@@ -702,6 +853,7 @@ int falx_create(int device, falx_ctx **out) {
     falx_ctx *c = new (std::nothrow) falx_ctx;
     if (!c) return FALX_ERR_INVALID;
     c->device = device;
+    if (const char *e = getenv("FALX_CTAS_PER_SM")) c->ctas_per_sm = atoi(e);
     int rc = FALX_OK;
     if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) rc = FALX_ERR_CUDA;
 #define FALX_SETUP(D)                                  \

@@ -21,6 +21,8 @@ constexpr int kHaloBytes = 1024;    // bytes staged after each tile
 constexpr int kMaxCols = 32;
 constexpr int kLocalRows = 2048;    // rows per tile with shared-memory validity staging
 constexpr int kVWords = kLocalRows / 64 + 2;
+constexpr int kRowCap = kLocalRows; // rows per tile on the data-parallel path
+constexpr int kTermCap = 4096;      // terminators per tile (+ halo) on the data-parallel path
 
 struct RowSpec {
     int ncols;
@@ -54,6 +56,13 @@ struct RowShared<true> {
     uint32_t warp_len[kWarps][kMaxStr];
     uint32_t arena_base[kMaxStr];
     uint32_t tile_len[kMaxStr];
+    // data-parallel path: per row its start (tile-relative), its first
+    // structural and its terminator ordinal; per terminator its structural
+    uint16_t row_pos[kRowCap];
+    uint16_t row_k[kRowCap];
+    uint16_t row_t[kRowCap];
+    uint16_t term_k[kTermCap];
+    uint32_t fast;
 };
 
 struct RowCtx {
@@ -252,9 +261,294 @@ __device__ __forceinline__ void stat_cell(StatAcc &a, int k, const uint8_t *s, u
     else a.inexact[k]++;
 }
 
+// String-arena look-back (one warp): returns, for each string column slot,
+// the arena bytes of the file before this tile; publishes the tile's totals.
+__device__ void arena_lookback(const RowCtx &rc, const uint32_t (&tot)[kMaxStr], int lane,
+                               unsigned long long (&pre)[kMaxStr]) {
+    ArenaStatusView *as = static_cast<ArenaStatusView *>(rc.astatus);
+    ArenaStatusView *me = &as[rc.tile];
+    if (lane == 0) {
+        for (int k = 0; k < kMaxStr; k++) me->agg[k] = tot[k];
+        st_release(&me->flag, rc.epoch * 4 + 1);
+    }
+    __syncwarp();
+    for (int k = 0; k < kMaxStr; k++) pre[k] = 0;
+    const uint64_t t0 = globaltimer_ns();
+    for (int64_t hi = (int64_t)rc.tile - 1; hi >= 0; hi -= 32) {
+        const int64_t j = hi - lane;
+        const bool in = j >= 0;
+        uint32_t flag = 0, ball_incl = 0;
+        bool gave_up = false;
+        for (uint32_t it = 0;; it++) {
+            if (in) flag = ld_acquire(&as[j].flag);
+            const bool cur = (flag >> 2) == rc.epoch;
+            const uint32_t not_ready = __ballot_sync(0xffffffffu, in && !(cur && (flag & 3) >= 1));
+            ball_incl = __ballot_sync(0xffffffffu, in && cur && (flag & 3) == 2);
+            const int first_incl = ball_incl ? __ffs(ball_incl) - 1 : 32;
+            const int first_wait = not_ready ? __ffs(not_ready) - 1 : 32;
+            if (first_wait > first_incl || not_ready == 0) break;
+            if ((it & 63) == 63) {
+                const bool stop = lane == 0 && (*(volatile uint32_t *)rc.hdr_abort ||
+                                                globaltimer_ns() - t0 > 4000000000ull);
+                if (__any_sync(0xffffffffu, stop)) {
+                    gave_up = true;
+                    break;
+                }
+            }
+            __nanosleep(32);
+        }
+        if (gave_up) {
+            if (lane == 0) {
+                atomicOr(rc.hdr_error, 1u);
+                atomicExch(rc.hdr_abort, 1u);
+            }
+            break;
+        }
+        const int sidx = ball_incl ? __ffs(ball_incl) - 1 : 32;
+        for (int k = 0; k < kMaxStr; k++) {
+            uint32_t v = 0;
+            if (in && lane < sidx) v = ld_relaxed(&as[j].agg[k]);
+            else if (in && lane == sidx) v = ld_relaxed(&as[j].incl[k]);
+            unsigned long long vv = v;
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) vv += __shfl_xor_sync(0xffffffffu, vv, d);
+            pre[k] += vv;
+        }
+        if (ball_incl) break;
+    }
+    if (lane == 0) {
+        bool over = false;
+        for (int k = 0; k < kMaxStr; k++) {
+            const unsigned long long inc = pre[k] + tot[k];
+            if (inc > 0x7FFFFFFFull) over = true;
+            me->incl[k] = (uint32_t)inc;
+        }
+        st_release(&me->flag, rc.epoch * 4 + 2);
+        if (over) atomicOr(rc.hdr_error, 2u);
+        if (rc.last_tile)
+            for (int k = 0; k < kMaxStr; k++) rc.hdr_arena[k] = pre[k] + tot[k];
+    }
+}
+
+// Block reduction of the sink accumulators into the call totals.
+__device__ void reduce_sinks(const RowSpec &rs, const RowCtx &rc, RowShared<true> &sh, const StatAcc &acc, int tid) {
+    const int lane = tid & 31, warp = tid >> 5;
+    unsigned long long v[11] = {acc.fields, acc.bytes, acc.records, acc.values[0], acc.values[1],
+                                acc.checksum[0], acc.checksum[1], acc.sum_e6[0], acc.sum_e6[1],
+                                acc.inexact[0], acc.inexact[1]};
+#pragma unroll
+    for (int k = 0; k < 11; k++) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], d);
+        if (lane == 0) sh.red[warp][k] = v[k];
+    }
+    __syncthreads();
+    if (tid < 11) {
+        unsigned long long t = 0;
+        for (int w = 0; w < kWarps; w++) t += sh.red[w][tid];
+        if (t) {
+            if (tid < 2) atomicAdd(&rc.hdr_fb[tid], t);
+            else atomicAdd(&rc.hdr_st[tid - 2], t);
+        }
+    }
+}
+
+// Span of field `f` of row `r` on the data-parallel path.
+struct Cell {
+    int64_t from, to;
+    bool present;
+};
+
+__device__ __forceinline__ Cell cell_span(const RowCtx &rc, const RowShared<true> &sh, const uint16_t *stage,
+                                          uint32_t n_total, uint32_t n_term_all, uint32_t r, uint32_t f) {
+    Cell c;
+    const uint32_t k0 = sh.row_k[r];
+    const uint32_t t = sh.row_t[r];
+    const bool closed = t < n_term_all;
+    const uint32_t kt = closed ? sh.term_k[t] : n_total;  // EOF rows: all remaining entries are separators
+    const uint32_t nf = kt - k0 + (closed ? 1 : 1);
+    const int64_t row0 = rc.vs + sh.row_pos[r];
+    c.present = f < nf;
+    if (!c.present) {
+        c.from = c.to = 0;
+        return c;
+    }
+    c.from = f == 0 ? row0 : rc.vs + (stage[k0 + f - 1] & 0x7FFF) + 1;
+    if (f + 1 == nf) {
+        int64_t to = closed ? rc.vs + (stage[kt] & 0x7FFF) : rc.len;
+        if (to > c.from && cell_ptr(rc, to - 1, to)[0] == '\r') to--;
+        c.to = to;
+    } else {
+        c.to = rc.vs + (stage[k0 + f] & 0x7FFF);
+    }
+    return c;
+}
+
+// Data-parallel row phase for ordinary tiles: the work is spread over
+// (row, column) cells and structural entries instead of per-thread walks.
+template <int D>
+__device__ void rows_fast(const RowSpec &rs, const RowCtx &rc, RowShared<true> &sh, const uint16_t *stage,
+                          uint32_t nrows, uint32_t nterm_tile, bool tile_rec0, int tid) {
+    const int lane = tid & 31, warp = tid >> 5;
+    const uint32_t n_total = rc.n_tile + sh.n_halo;
+    const bool last_open = nrows > 0 && sh.row_t[nrows - 1] == nterm_tile;
+    const uint32_t n_term_all = nterm_tile + (last_open && sh.halo_kind == 0 ? 1u : 0u);
+    const uint32_t vshift = rc.row_base & 63;
+    StatAcc acc = {};
+
+    // ---- string lengths: thread t owns rows [t*chunk, (t+1)*chunk)
+    const uint32_t chunk = (nrows + kThreads - 1) / kThreads;
+    const uint32_t r0 = min(nrows, tid * chunk), r1 = min(nrows, r0 + chunk);
+    uint32_t slen[kMaxStr] = {0, 0, 0, 0};
+    if (rs.nstr > 0) {
+        for (int c = 0; c < rs.ncols; c++) {
+            if (rs.type[c] != 3) continue;
+            const int k = rs.str_slot[c];
+            for (uint32_t r = r0; r < r1; r++) {
+                const Cell cl = cell_span(rc, sh, stage, n_total, n_term_all, r, rs.field[c]);
+                if (cl.present) slen[k] += cleaned_len(cell_ptr(rc, cl.from, cl.to), (uint32_t)(cl.to - cl.from));
+            }
+        }
+        for (int k = 0; k < kMaxStr; k++) {
+            uint32_t x = slen[k], xi = x;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                uint32_t o = __shfl_up_sync(0xffffffffu, xi, d);
+                if (lane >= d) xi += o;
+            }
+            if (lane == 31) sh.warp_len[warp][k] = xi;
+            slen[k] = xi - x;  // exclusive within the warp
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int k = 0; k < kMaxStr; k++) {
+                uint32_t run = 0;
+                for (int w = 0; w < kWarps; w++) {
+                    uint32_t t = sh.warp_len[w][k];
+                    sh.warp_len[w][k] = run;
+                    run += t;
+                }
+                sh.tile_len[k] = run;
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- numeric / bytes / validity: warps take 32 consecutive rows of one column
+    const uint32_t rpad = (nrows + 31) & ~31u;
+    const uint32_t ncell = rpad * (uint32_t)rs.ncols;
+    for (uint32_t i = tid; i < ncell; i += kThreads) {
+        const int c = (int)(i / rpad);
+        const uint32_t r = i % rpad;
+        bool ok = false;
+        if (r < nrows) {
+            const uint64_t g = (uint64_t)rc.row_base + r;
+            const Cell cl = cell_span(rc, sh, stage, n_total, n_term_all, r, rs.field[c]);
+            uint32_t dummy[kMaxStr] = {0, 0, 0, 0};
+            const uint32_t n = (uint32_t)(cl.to - cl.from);
+            ok = decode_cell(rs, c, g, cl.present ? cell_ptr(rc, cl.from, cl.to) : nullptr, n, cl.present, cl.from,
+                             cl.to, dummy);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+        if (lane == 0 && bal) {
+            const uint32_t bo = vshift + (r - lane);
+            const uint32_t w = bo >> 6, sh6 = bo & 63;
+            atomicOr((unsigned long long *)&sh.vbits[c][w], (unsigned long long)bal << sh6);
+            if (sh6 > 32) atomicOr((unsigned long long *)&sh.vbits[c][w + 1], (unsigned long long)bal >> (64 - sh6));
+        }
+    }
+
+    // ---- count / sum sink over two fields
+    if (rs.want_stats) {
+        for (uint32_t i = tid; i < 2 * nrows; i += kThreads) {
+            const int k = i >= nrows ? 1 : 0;
+            const uint32_t r = i - k * nrows;
+            const Cell cl = cell_span(rc, sh, stage, n_total, n_term_all, r, rs.stats_field[k]);
+            if (cl.present) stat_cell(acc, k, cell_ptr(rc, cl.from, cl.to), (uint32_t)(cl.to - cl.from));
+        }
+        if (tid == 0) acc.records += nrows;
+    }
+
+    // ---- field bytes: one structural entry per field
+    if (rs.want_fb) {
+        uint32_t first = 0;
+        if (!tile_rec0) first = nterm_tile > 0 ? (uint32_t)sh.term_k[0] + 1 : n_total;
+        const uint32_t last = last_open ? n_total : (nterm_tile > 0 ? (uint32_t)sh.term_k[nterm_tile - 1] + 1 : 0);
+        const int64_t rec0 = rc.vs > 0 ? rc.vs : 0;
+        for (uint32_t i = first + tid; i < last; i += kThreads) {
+            const uint16_t e = stage[i];
+            const int64_t pos = rc.vs + (e & 0x7FFF);
+            const bool starts_rec = i == 0 || (stage[i - 1] >> 15);
+            const int64_t from = i == 0 ? rec0 : rc.vs + (stage[i - 1] & 0x7FFF) + 1;
+            int64_t to = pos;
+            if (e >> 15) {
+                if (D == D_CSV_HASH && starts_rec && to > from && cell_ptr(rc, from, from + 1)[0] == '#') continue;
+                if (to > from && cell_ptr(rc, to - 1, to)[0] == '\r') to--;
+            }
+            acc.fields++;
+            acc.bytes += cleaned_len(cell_ptr(rc, from, to), (uint32_t)(to - from));
+        }
+        // a last row without terminator ends its last field at end of file
+        if (tid == 0 && last_open && n_term_all == nterm_tile) {
+            const uint32_t k0 = sh.row_k[nrows - 1];
+            const int64_t from = n_total > k0 ? rc.vs + (stage[n_total - 1] & 0x7FFF) + 1 : rc.vs + sh.row_pos[nrows - 1];
+            int64_t to = rc.len;
+            if (to > from && cell_ptr(rc, to - 1, to)[0] == '\r') to--;
+            acc.fields++;
+            acc.bytes += cleaned_len(cell_ptr(rc, from, to), (uint32_t)(to - from));
+        }
+    }
+
+    // ---- string arenas: look-back for the tile's arena offsets, then copy
+    if (rs.nstr > 0 && warp == 0) {
+        uint32_t tot[kMaxStr];
+        for (int k = 0; k < kMaxStr; k++) tot[k] = sh.tile_len[k];
+        unsigned long long pre[kMaxStr];
+        arena_lookback(rc, tot, lane, pre);
+        if (lane == 0)
+            for (int k = 0; k < kMaxStr; k++) sh.arena_base[k] = (uint32_t)pre[k];
+    }
+    __syncthreads();
+
+    // validity words (row bits staged relative to the tile's first row)
+    {
+        const uint64_t w0 = (uint64_t)rc.row_base >> 6;
+        const uint64_t maxw = (rs.rows_cap + 63) / 64;
+        for (int i = tid; i < rs.ncols * kVWords; i += kThreads) {
+            const int c = i / kVWords, wi = i % kVWords;
+            const uint64_t v = sh.vbits[c][wi];
+            if (v && w0 + wi < maxw) atomicOr((unsigned long long *)&rs.valid[c][w0 + wi], (unsigned long long)v);
+        }
+    }
+    if (rs.want_fb || rs.want_stats) reduce_sinks(rs, rc, sh, acc, tid);
+
+    if (rs.nstr > 0) {
+        if (rc.tile == 0 && tid == 0)
+            for (int c = 0; c < rs.ncols; c++)
+                if (rs.type[c] == 3) static_cast<int32_t *>(rs.values[c])[0] = 0;
+        for (int c = 0; c < rs.ncols; c++) {
+            if (rs.type[c] != 3) continue;
+            const int k = rs.str_slot[c];
+            uint64_t at = (uint64_t)sh.arena_base[k] + sh.warp_len[warp][k] + slen[k];
+            for (uint32_t r = r0; r < r1; r++) {
+                const uint64_t g = (uint64_t)rc.row_base + r;
+                const Cell cl = cell_span(rc, sh, stage, n_total, n_term_all, r, rs.field[c]);
+                if (cl.present) {
+                    const uint32_t n = (uint32_t)(cl.to - cl.from);
+                    const uint8_t *src = cell_ptr(rc, cl.from, cl.to);
+                    copy_clean(src, n, rs.str_data[c], at, rs.str_cap[c]);
+                    at += cleaned_len(src, n);
+                }
+                if (g < rs.rows_cap) static_cast<int32_t *>(rs.values[c])[g + 1] = (int32_t)at;
+            }
+        }
+    }
+}
+
 template <int D>
 __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> &sh, uint16_t *stage,
-                           uint64_t rows_m, uint64_t stm, uint64_t term, uint32_t excl_struct, uint32_t excl_rows,
+                           uint64_t rows_m, uint64_t stm, uint64_t term, uint32_t excl_struct, uint32_t excl_term,
+                           uint32_t excl_rows, uint32_t nterm_tile, uint32_t nrows_tile, bool tile_rec0,
                            int64_t base_t, int tid) {
     const int lane = tid & 31, warp = tid >> 5;
     const int64_t ve = rc.vs + kTile;
@@ -272,6 +566,29 @@ __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> 
         sh.high_fields = hf;
     }
     for (int i = tid; i < rs.ncols * kVWords; i += kThreads) sh.vbits[i / kVWords][i % kVWords] = 0;
+
+    // ---- row and terminator tables for the data-parallel path
+    const bool tables = nrows_tile <= (uint32_t)kRowCap && nterm_tile < (uint32_t)kTermCap;
+    if (tables) {
+        uint64_t mm = rows_m;
+        uint32_t r = excl_rows;
+        while (mm) {
+            const unsigned b = __ffsll((long long)mm) - 1;
+            mm &= mm - 1;
+            const uint64_t below = (1ull << b) - 1;
+            sh.row_pos[r] = (uint16_t)(base_t - rc.vs + b);
+            sh.row_k[r] = (uint16_t)(excl_struct + __popcll(stm & below));
+            sh.row_t[r] = (uint16_t)(excl_term + __popcll(term & below));
+            r++;
+        }
+        uint64_t tm = term;
+        while (tm) {
+            const unsigned b = __ffsll((long long)tm) - 1;
+            sh.term_k[excl_term + __popcll(term & ((1ull << b) - 1))] =
+                (uint16_t)(excl_struct + __popcll(stm & ((1ull << b) - 1)));
+            tm &= tm - 1;
+        }
+    }
 
     // ---- halo: structurals after the tile up to the first terminator
     if (warp == 0) {
@@ -341,9 +658,16 @@ __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> 
             sh.n_halo = n_halo;
             sh.halo_kind = kind;
             sh.halo_exit = hexit;
+            if (tables && kind == 0 && n_halo > 0) sh.term_k[nterm_tile] = (uint16_t)(rc.n_tile + n_halo - 1);
+            const bool last_open = nrows_tile > 0 && tables && sh.row_t[nrows_tile - 1] == nterm_tile;
+            sh.fast = tables && !(last_open && kind == 2);
         }
     }
     __syncthreads();
+    if (sh.fast) {
+        rows_fast<D>(rs, rc, sh, stage, nrows_tile, nterm_tile, tile_rec0, tid);
+        return;
+    }
 
     // ---- per-thread rows
     StatAcc acc = {};
@@ -471,57 +795,86 @@ __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> 
             excl_len[k] = xi - x;
         }
         __syncthreads();
-        if (tid == 0) {
+        if (warp == 0) {
             uint32_t tot[kMaxStr];
             for (int k = 0; k < kMaxStr; k++) {
                 uint32_t run = 0;
-                for (int w = 0; w < kWarps; w++) {
-                    uint32_t t = sh.warp_len[w][k];
-                    sh.warp_len[w][k] = run;
-                    run += t;
-                }
+                for (int w = 0; w < kWarps; w++) run += sh.warp_len[w][k];
                 tot[k] = run;
-                sh.tile_len[k] = run;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                for (int k = 0; k < kMaxStr; k++) {
+                    uint32_t run = 0;
+                    for (int w = 0; w < kWarps; w++) {
+                        uint32_t t = sh.warp_len[w][k];
+                        sh.warp_len[w][k] = run;
+                        run += t;
+                    }
+                    sh.tile_len[k] = run;
+                }
             }
             ArenaStatusView *as = static_cast<ArenaStatusView *>(rc.astatus);
             ArenaStatusView *me = &as[rc.tile];
-            for (int k = 0; k < kMaxStr; k++) me->agg[k] = tot[k];
-            st_release(&me->flag, rc.epoch * 4 + 1);
+            if (lane == 0) {
+                for (int k = 0; k < kMaxStr; k++) me->agg[k] = tot[k];
+                st_release(&me->flag, rc.epoch * 4 + 1);
+            }
+            __syncwarp();
             unsigned long long pre[kMaxStr] = {0, 0, 0, 0};
-            for (int64_t j = (int64_t)rc.tile - 1; j >= 0; j--) {
-                uint32_t flag = 0, polls = 0;
+            for (int64_t hi = (int64_t)rc.tile - 1; hi >= 0; hi -= 32) {
+                const int64_t j = hi - lane;
+                const bool in = j >= 0;
+                uint32_t flag = 0;
                 bool gave_up = false;
                 const uint64_t t0 = globaltimer_ns();
-                for (;;) {
-                    flag = ld_acquire(&as[j].flag);
-                    if ((flag >> 2) == rc.epoch && (flag & 3) >= 1) break;
-                    if ((++polls & 255) == 0 &&
-                        (*(volatile uint32_t *)rc.hdr_abort || globaltimer_ns() - t0 > 4000000000ull)) {
+                for (uint32_t it = 0;; it++) {
+                    if (in) flag = ld_acquire(&as[j].flag);
+                    bool ready = !in || ((flag >> 2) == rc.epoch && (flag & 3) >= 1);
+                    if (__all_sync(0xffffffffu, ready)) break;
+                    if ((it & 63) == 63) {
+                        bool stop = lane == 0 && (*(volatile uint32_t *)rc.hdr_abort ||
+                                                  globaltimer_ns() - t0 > 4000000000ull);
+                        if (__any_sync(0xffffffffu, stop)) {
+                            gave_up = true;
+                            break;
+                        }
+                    }
+                    __nanosleep(32);
+                }
+                if (gave_up) {
+                    if (lane == 0) {
                         atomicOr(rc.hdr_error, 1u);
                         atomicExch(rc.hdr_abort, 1u);
-                        gave_up = true;
-                        break;
                     }
-                    __nanosleep(64);
-                }
-                if (gave_up) break;
-                if ((flag & 3) == 2) {
-                    for (int k = 0; k < kMaxStr; k++) pre[k] += ld_relaxed(&as[j].incl[k]);
                     break;
                 }
-                for (int k = 0; k < kMaxStr; k++) pre[k] += ld_relaxed(&as[j].agg[k]);
+                const uint32_t ball = __ballot_sync(0xffffffffu, in && (flag & 3) == 2);
+                const int sidx = ball ? __ffs(ball) - 1 : 32;
+                for (int k = 0; k < kMaxStr; k++) {
+                    uint32_t v = 0;
+                    if (in && lane < sidx) v = ld_relaxed(&as[j].agg[k]);
+                    else if (in && lane == sidx) v = ld_relaxed(&as[j].incl[k]);
+                    unsigned long long vv = v;
+#pragma unroll
+                    for (int d = 16; d > 0; d >>= 1) vv += __shfl_xor_sync(0xffffffffu, vv, d);
+                    pre[k] += vv;
+                }
+                if (ball) break;
             }
-            bool over = false;
-            for (int k = 0; k < kMaxStr; k++) {
-                unsigned long long inc = pre[k] + tot[k];
-                if (inc > 0x7FFFFFFFull) over = true;
-                me->incl[k] = (uint32_t)inc;
-                sh.arena_base[k] = (uint32_t)pre[k];
+            if (lane == 0) {
+                bool over = false;
+                for (int k = 0; k < kMaxStr; k++) {
+                    unsigned long long inc = pre[k] + tot[k];
+                    if (inc > 0x7FFFFFFFull) over = true;
+                    me->incl[k] = (uint32_t)inc;
+                    sh.arena_base[k] = (uint32_t)pre[k];
+                }
+                st_release(&me->flag, rc.epoch * 4 + 2);
+                if (over) atomicOr(rc.hdr_error, 2u);
+                if (rc.last_tile)
+                    for (int k = 0; k < kMaxStr; k++) rc.hdr_arena[k] = pre[k] + tot[k];
             }
-            st_release(&me->flag, rc.epoch * 4 + 2);
-            if (over) atomicOr(rc.hdr_error, 2u);
-            if (rc.last_tile)
-                for (int k = 0; k < kMaxStr; k++) rc.hdr_arena[k] = pre[k] + tot[k];
         }
         __syncthreads();
         uint64_t at[kMaxStr];
