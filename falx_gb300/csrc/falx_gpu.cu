@@ -140,6 +140,19 @@ __device__ __forceinline__ void issue_tile(const Params &p, uint32_t t, uint8_t 
     bulk_g2s(dst + (lo - lo_full), lo, bytes, bar);
 }
 
+// Bulk copy of tile `t` (plus the kPre bytes before it) for the index kernel.
+__device__ __forceinline__ void issue_tile_ix(const Params &p, uint32_t t, uint8_t *dst, uint64_t *bar) {
+    constexpr int kBuf = kPre + kTile;
+    const uint8_t *lo_full = p.abase + (uint64_t)t * kTile - kPre;
+    const uint8_t *lo = t == 0 ? p.abase : lo_full;
+    const uint8_t *end16 = p.abase + ((p.shift + p.len + 15) & ~15ull);
+    const uint8_t *hi = lo_full + kBuf;
+    if (hi > end16) hi = end16;
+    const uint32_t bytes = (uint32_t)(hi - lo);
+    mbar_expect_tx(bar, bytes);
+    bulk_g2s(dst + (lo - lo_full), lo, bytes, bar);
+}
+
 // Inclusive warp scan of transfer functions.
 __device__ __forceinline__ uint32_t warp_scan_f(uint32_t f, int lane) {
 #pragma unroll
@@ -464,7 +477,8 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uin
         while (mm) {
             unsigned bpos = __ffsll((long long)mm) - 1;
             uint32_t rel = (uint32_t)(tid * kThreadBytes + bpos);
-            S.stage[k++] = (uint16_t)(rel | (((term >> bpos) & 1) << 15));
+            if (k < (uint32_t)kTile) S.stage[k] = (uint16_t)(rel | (((term >> bpos) & 1) << 15));
+            k++;
             mm &= mm - 1;
         }
     }
@@ -523,6 +537,374 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uin
         const bool rec0 = vs <= 0 || (b[kPre - 1] == '\n' && state_outside<D>(entry));
         rows_phase<D>(p.rows, rc, S.rs, S.stage, rows_m, stm, term, cfield(ce, 0), cfield(ce, 1), cfield(ce, 2),
                       cfield(S.tile_c, 1), cfield(S.tile_c, 2), rec0, base_t, tid);
+    }
+}
+
+// ===========================================================================
+// Index / tape kernel with deferred look-back.
+//
+// Without rows, a tile's input is only read during its local pass, so its
+// buffer is refilled right after that pass and the tile's look-back and
+// output are deferred by one round: iteration i runs the local pass of tile
+// c + iG, then the look-back and output of tile c + (i-1)G. By then every
+// aggregate the look-back needs has been published, so it never waits on a
+// tile that is still classifying.
+// ===========================================================================
+struct LocalState {
+    Masks m;
+    uint64_t ls;
+    int64_t base_t;
+    uint32_t excl;
+    bool prev_nl;
+    unsigned long long cv[4];
+};
+
+struct SmemIx {
+    alignas(128) uint8_t buf[2][kPre + kTile];
+    uint16_t stage[kTile];
+    uint64_t bar[2];
+    uint32_t warp_f[kWarps];
+    unsigned long long warp_agg[kWarps][4];
+    unsigned long long warp_c[kWarps];
+    uint32_t tile_f, ptile_f;
+    unsigned long long agg[4], pagg[4];
+    // block-wide look-back
+    uint32_t lb_wf[kWarps];
+    unsigned long long lb_wc[kWarps][4];
+    uint32_t lb_first_incl[3], lb_first_wait[3], lb_stop, lb_entry, lb_pre[3];
+    uint32_t base[3];
+    unsigned long long tile_c;
+};
+
+// Local pass of one tile: classify, scan transfer functions, publish the
+// aggregate. Leaves the per-thread state needed by the deferred output.
+template <int D>
+__device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t tile, uint8_t *b, LocalState &L) {
+    constexpr int kBuf = kPre + kTile;
+    constexpr int NS = NStates<D>::value;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t vs = (int64_t)tile * kTile - (int64_t)p.shift;
+    const int64_t len = (int64_t)p.len;
+    if (vs - kPre < 0 || vs - kPre + kBuf > len) {
+        for (int i = tid; i < kBuf; i += kThreads) {
+            const int64_t v = vs - kPre + i;
+            if (v < 0 || v >= len) b[i] = 0;
+        }
+        __syncthreads();
+    }
+    const int r = (lane >> 1) & 3;
+    uint32_t w[16];
+    const uint4 *src = reinterpret_cast<const uint4 *>(b + kPre + tid * kThreadBytes);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const uint4 v = src[(k + r) & 3];
+        w[4 * k] = v.x; w[4 * k + 1] = v.y; w[4 * k + 2] = v.z; w[4 * k + 3] = v.w;
+    }
+    L.m = classify<D>(w, r);
+    L.base_t = vs + (int64_t)tid * kThreadBytes;
+    L.prev_nl = b[kPre + tid * kThreadBytes - 1] == '\n';
+    L.ls = (L.m.nl << 1) | (uint64_t)L.prev_nl;
+    if (L.base_t <= 0 && L.base_t + kThreadBytes > 0) L.ls |= 1ull << (-L.base_t);
+    const uint32_t f = thread_function<D>(L.m, L.ls);
+    uint32_t incl = warp_scan_f(f, lane);
+    if (lane == 31) S.warp_f[warp] = incl;
+    uint32_t excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = kIdentity;
+#pragma unroll
+    for (int e = 0; e < NS; e++) L.cv[e] = thread_counts<D, false>(L.m, L.ls, L.prev_nl, e, L.base_t, len);
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t wf = lane < kWarps ? S.warp_f[lane] : kIdentity;
+        const uint32_t wi = warp_scan_f(wf, lane);
+        uint32_t we = __shfl_up_sync(0xffffffffu, wi, 1);
+        if (lane == 0) we = kIdentity;
+        if (lane < kWarps) S.warp_f[lane] = we;
+        if (lane == kWarps - 1) S.tile_f = wi;
+    }
+    __syncthreads();
+    L.excl = fcompose(S.warp_f[warp], excl);
+    {
+        unsigned long long v[NS];
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++) {
+            const uint32_t e = fapply(L.excl, s0);
+            unsigned long long x = L.cv[0];
+#pragma unroll
+            for (int t = 1; t < NS; t++) x = e == (uint32_t)t ? L.cv[t] : x;
+            v[s0] = x;
+        }
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++) {
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) v[s0] += __shfl_xor_sync(0xffffffffu, v[s0], d);
+            if (lane == 0) S.warp_agg[warp][s0] = v[s0];
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        TileStatus *tst = &p.status[tile];
+        unsigned long long agg[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++)
+            for (int w2 = 0; w2 < kWarps; w2++) agg[s0] += S.warp_agg[w2][s0];
+        tst->func = S.tile_f;
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++) tst->agg[s0] = agg[s0];
+        st_release(&tst->flag, p.epoch * 4 + 1);
+        for (int s0 = 0; s0 < 4; s0++) S.agg[s0] = agg[s0];
+    }
+}
+
+// Block-wide look-back (all threads): thread t watches predecessor
+// tile - 1 - t. Waits only for the predecessors nearer than the nearest
+// published inclusive prefix.
+template <int NS>
+__device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t &entry, uint32_t pre[3]) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t af = kIdentity;  // thread 0: aggregate between the window and `tile`
+    uint64_t ac[4] = {0, 0, 0, 0};
+    const uint64_t t0 = globaltimer_ns();
+    if (tile == 0) {
+        entry = 0;
+        pre[0] = pre[1] = pre[2] = 0;
+        return;
+    }
+    for (int64_t hi = (int64_t)tile - 1; hi >= 0; hi -= kThreads) {
+        const int64_t j = hi - tid;
+        const bool in = j >= 0;
+        uint32_t flag = 0;
+        uint32_t sidx;
+        // Three rotating slots for the block-wide minima: in poll iteration
+        // `it` thread 0 resets slot it+1 before the barrier, every thread
+        // updates slot it before it and reads slot it after it. No slot is
+        // reset while a thread may still read it.
+        if (tid == 0) {
+            S.lb_first_incl[0] = S.lb_first_wait[0] = kThreads;
+        }
+        __syncthreads();
+        for (uint32_t it = 0;; it++) {
+            const uint32_t sl = it % 3, nx = (it + 1) % 3;
+            if (tid == 0) S.lb_first_incl[nx] = S.lb_first_wait[nx] = kThreads;
+            if (in) flag = ld_acquire(&p.status[j].flag);
+            const bool cur = (flag >> 2) == p.epoch;
+            const bool waitv = in && !(cur && (flag & 3) >= 1);
+            const bool incl = in && cur && (flag & 3) >= 2;
+            const uint32_t bw = __ballot_sync(0xffffffffu, waitv), bi = __ballot_sync(0xffffffffu, incl);
+            if (lane == 0 && bw) atomicMin(&S.lb_first_wait[sl], (uint32_t)(warp * 32 + __ffs(bw) - 1));
+            if (lane == 0 && bi) atomicMin(&S.lb_first_incl[sl], (uint32_t)(warp * 32 + __ffs(bi) - 1));
+            __syncthreads();
+            const uint32_t fw = S.lb_first_wait[sl], fi = S.lb_first_incl[sl];
+            sidx = fi;
+            if (fw > fi || fw == (uint32_t)kThreads) break;
+            if ((it & 15) == 15) {
+                const bool stop = tid == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
+                if (__syncthreads_or(stop)) {
+                    if (tid == 0) fail(p.hdr, ERR_TIMEOUT);
+                    entry = 0;
+                    pre[0] = pre[1] = pre[2] = 0;
+                    return;
+                }
+            }
+            __nanosleep(64);
+        }
+        uint32_t f = kIdentity;
+        uint64_t c[4] = {0, 0, 0, 0};
+        if (in && (uint32_t)tid < sidx) {
+            f = ld_relaxed(&p.status[j].func);
+#pragma unroll
+            for (int s0 = 0; s0 < NS; s0++) c[s0] = ld_relaxed64(&p.status[j].agg[s0]);
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t gf = __shfl_down_sync(0xffffffffu, f, d);
+            uint64_t gc[4];
+#pragma unroll
+            for (int s0 = 0; s0 < NS; s0++) gc[s0] = __shfl_down_sync(0xffffffffu, c[s0], d);
+            if (lane + d < 32) agg_prepend<NS>(gf, gc, f, c);
+        }
+        if (lane == 0) {
+            S.lb_wf[warp] = f;
+#pragma unroll
+            for (int s0 = 0; s0 < NS; s0++) S.lb_wc[warp][s0] = c[s0];
+        }
+        if ((uint32_t)tid == sidx) {
+            S.lb_entry = ld_relaxed(&p.status[j].exit);
+            S.lb_pre[0] = ld_relaxed(&p.status[j].incl[0]);
+            S.lb_pre[1] = ld_relaxed(&p.status[j].incl[1]);
+            S.lb_pre[2] = ld_relaxed(&p.status[j].incl[2]);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t wf = kIdentity;
+            uint64_t wc[4] = {0, 0, 0, 0};
+            for (int w = 0; w < kWarps; w++) {
+                uint64_t g[4];
+#pragma unroll
+                for (int s0 = 0; s0 < NS; s0++) g[s0] = S.lb_wc[w][s0];
+                agg_prepend<NS>(S.lb_wf[w], g, wf, wc);
+            }
+            agg_prepend<NS>(wf, wc, af, ac);
+            const bool found = sidx < (uint32_t)kThreads;
+            const bool at_start = hi - kThreads < 0;
+            S.lb_stop = found || at_start;
+            if (found) {
+                const uint32_t ex = S.lb_entry;
+                uint64_t cc = ac[0];
+#pragma unroll
+                for (int t = 1; t < NS; t++) cc = ex == (uint32_t)t ? ac[t] : cc;
+                S.lb_pre[0] += cfield(cc, 0);
+                S.lb_pre[1] += cfield(cc, 1);
+                S.lb_pre[2] += cfield(cc, 2);
+                S.lb_entry = fapply(af, ex);
+            } else if (at_start) {
+                S.lb_pre[0] = cfield(ac[0], 0);
+                S.lb_pre[1] = cfield(ac[0], 1);
+                S.lb_pre[2] = cfield(ac[0], 2);
+                S.lb_entry = fapply(af, 0);
+            }
+        }
+        __syncthreads();
+        if (S.lb_stop) break;
+    }
+    entry = S.lb_entry;
+    pre[0] = S.lb_pre[0];
+    pre[1] = S.lb_pre[1];
+    pre[2] = S.lb_pre[2];
+}
+
+// Deferred output of one tile: inclusive prefix, staged index, tape.
+template <int D>
+__device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t tile, const LocalState &L) {
+    constexpr int NS = NStates<D>::value;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t vs = (int64_t)tile * kTile - (int64_t)p.shift;
+    uint32_t entry, pre[3];
+    lookback_cta<NS>(p, S, tile, entry, pre);
+    if (tid == 0) {
+        TileStatus *tst = &p.status[tile];
+        unsigned long long mine = S.pagg[0];
+#pragma unroll
+        for (int t = 1; t < NS; t++) mine = entry == (uint32_t)t ? S.pagg[t] : mine;
+        tst->exit = fapply(S.ptile_f, entry);
+        tst->incl[0] = pre[0] + cfield(mine, 0);
+        tst->incl[1] = pre[1] + cfield(mine, 1);
+        tst->incl[2] = pre[2] + cfield(mine, 2);
+        st_release(&tst->flag, p.epoch * 4 + 2);
+        S.tile_c = mine;
+        if (tile == p.num_tiles - 1) {
+            p.hdr->n_struct = pre[0] + cfield(mine, 0);
+            p.hdr->n_terms = pre[1] + cfield(mine, 1);
+            p.hdr->n_rows = pre[2] + cfield(mine, 2);
+        }
+    }
+    const uint32_t s_in = fapply(L.excl, entry);
+    const uint64_t stm = structural_mask<D>(L.m, L.ls, s_in);
+    const uint64_t term = stm & L.m.nl;
+    unsigned long long c = L.cv[0];
+#pragma unroll
+    for (int t = 1; t < NS; t++) c = s_in == (uint32_t)t ? L.cv[t] : c;
+    const unsigned long long ci = warp_scan_sum(c, lane);
+    if (lane == 31) S.warp_c[warp] = ci;
+    unsigned long long ce = ci - c;
+    __syncthreads();
+    if (warp == 0) {
+        const unsigned long long wc = lane < kWarps ? S.warp_c[lane] : 0ull;
+        const unsigned long long wi = warp_scan_sum(wc, lane);
+        if (lane < kWarps) S.warp_c[lane] = wi - wc;
+    }
+    __syncthreads();
+    ce += S.warp_c[warp];
+    {
+        uint32_t k = cfield(ce, 0);
+        uint64_t mm = stm;
+        while (mm) {
+            const unsigned bpos = __ffsll((long long)mm) - 1;
+            if (k < (uint32_t)kTile) S.stage[k] = (uint16_t)(tid * kThreadBytes + bpos);
+            k++;
+            mm &= mm - 1;
+        }
+    }
+    __syncthreads();
+    const uint32_t n_tile = min(cfield(S.tile_c, 0), (uint32_t)kTile);
+    if (p.index) {
+        for (uint32_t i = tid; i < n_tile; i += kThreads) {
+            const uint64_t g = (uint64_t)pre[0] + i;
+            if (g < p.index_cap) p.index[g] = (uint32_t)(vs + S.stage[i]);
+        }
+    }
+    if (p.seps || p.ends) {
+        const uint32_t my_s = cfield(ce, 0), my_t = cfield(ce, 1);
+        uint64_t sep_before = (uint64_t)(pre[0] - pre[1]) + (my_s - my_t);
+        uint64_t term_before = (uint64_t)pre[1] + my_t;
+        uint64_t mm = stm;
+        while (mm) {
+            const unsigned bpos = __ffsll((long long)mm) - 1;
+            const uint64_t pos = (uint64_t)(L.base_t + bpos);
+            if ((term >> bpos) & 1) {
+                if (p.ends && term_before < p.ends_cap) p.ends[term_before] = (sep_before << 32) | pos;
+                term_before++;
+            } else {
+                if (p.seps && sep_before < p.seps_cap) p.seps[sep_before] = (uint32_t)pos;
+                sep_before++;
+            }
+            mm &= mm - 1;
+        }
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) index_kernel(const Params p) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    SmemIx &S = *reinterpret_cast<SmemIx *>(smem_raw);
+    const int tid = threadIdx.x;
+    const uint32_t G = gridDim.x;
+    if (tid == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        fence_mbar_init();
+        for (int s = 0; s < 2; s++) {
+            const uint32_t t = blockIdx.x + (uint32_t)s * G;
+            if (t < p.num_tiles) issue_tile_ix(p, t, S.buf[s], &S.bar[s]);
+        }
+    }
+    __syncthreads();
+    uint32_t phase[2] = {0, 0};
+    LocalState prev;
+    bool have_prev = false;
+    uint32_t prev_tile = 0;
+    for (uint32_t i = 0;; i++) {
+        const uint32_t tile = blockIdx.x + i * G;
+        const int s = i & 1;
+        const bool has_cur = tile < p.num_tiles;
+        LocalState cur;
+        if (has_cur) {
+            const bool ok = mbar_wait(&S.bar[s], phase[s], kWaitNs);
+            if (__syncthreads_or(!ok || (tid == 0 && aborted(p.hdr)))) {
+                if (tid == 0) {
+                    if (!ok) fail(p.hdr, ERR_TMA);
+                    else if (tile + G < p.num_tiles) mbar_wait(&S.bar[s ^ 1], phase[s ^ 1], kWaitNs);
+                }
+                break;
+            }
+            phase[s] ^= 1;
+            local_pass<D>(p, S, tile, S.buf[s], cur);
+            __syncthreads();  // buf[s] fully read
+            if (tid == 0 && tile + 2 * G < p.num_tiles) {
+                fence_proxy_async();
+                issue_tile_ix(p, tile + 2 * G, S.buf[s], &S.bar[s]);
+            }
+        }
+        if (have_prev) output_pass<D>(p, S, prev_tile, prev);
+        if (!has_cur) break;
+        __syncthreads();
+        if (tid == 0) {
+            S.ptile_f = S.tile_f;
+            for (int k = 0; k < 4; k++) S.pagg[k] = S.agg[k];
+        }
+        __syncthreads();
+        prev = cur;
+        prev_tile = tile;
+        have_prev = true;
     }
 }
 
@@ -617,10 +999,11 @@ int cuda_fail(cudaError_t e) {
 
 template <int D, bool ROWS>
 int setup_kernel(falx_ctx *c) {
-    size_t smem = sizeof(Smem<ROWS>);
-    FALX_CUDA(cudaFuncSetAttribute(scan_kernel<D, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const void *fn = ROWS ? (const void *)scan_kernel<D, true> : (const void *)index_kernel<D>;
+    const size_t smem = ROWS ? sizeof(Smem<true>) : sizeof(SmemIx);
+    FALX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nb = 0;
-    FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<D, ROWS>, kThreads, smem));
+    FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
     c->blocks_per_sm[D][ROWS] = nb > 0 ? nb : 1;
     return FALX_OK;
 }
@@ -678,8 +1061,8 @@ int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t 
             err = cudaLaunchCooperativeKernel((const void *)scan_kernel<D, true>, dim3((unsigned)grid), \
                                               dim3(kThreads), args_, sizeof(Smem<true>), c->stream);     \
         else                                                                                      \
-            err = cudaLaunchCooperativeKernel((const void *)scan_kernel<D, false>, dim3((unsigned)grid), \
-                                              dim3(kThreads), args_, sizeof(Smem<false>), c->stream);    \
+            err = cudaLaunchCooperativeKernel((const void *)index_kernel<D>, dim3((unsigned)grid),     \
+                                              dim3(kThreads), args_, sizeof(SmemIx), c->stream);         \
     } while (0)
     cudaError_t err = cudaSuccess;
     switch (dialect) {

@@ -74,3 +74,26 @@ def test_parse_i64(cell, expect):
 ])
 def test_parse_u32(cell, expect):
     assert oracle.parse_u32(cell) == expect
+
+
+@pytest.mark.parametrize("kind,dialect", [(1, 1), (0, 0), (3, 2), (5, 1)])
+def test_parallel_port_matches_serial(kind, dialect):
+    # The timed CPU baseline (the port of the reference's _par drivers)
+    # must agree with the serial restatement at every thread count.
+    from falx_gb300 import gen
+
+    doc = gen.generate(kind, 2 << 20)
+    cols = [(0, oracle.U32), (1, oracle.STR), (3, oracle.U32), (4, oracle.F64), (5, oracle.F64)]
+    serial_rows, serial_cols = oracle.parse_columns(doc, dialect, cols)
+    for threads in (1, 2, 3, 7, 16):
+        assert np.array_equal(oracle.index_par(doc, dialect, threads), oracle.index_spec(doc, dialect))
+        assert oracle.field_bytes(doc, dialect, par_threads=threads) == oracle.field_bytes(doc, dialect)
+        rows, got = oracle.parse_columns(doc, dialect, cols, par_threads=threads)
+        assert rows == serial_rows
+        for k in range(len(cols)):
+            for key, v in serial_cols[k].items():
+                g = got[k][key]
+                if isinstance(v, bytes):
+                    assert g == v
+                else:
+                    assert np.array_equal(np.asarray(g).view(np.uint8), np.asarray(v).view(np.uint8))
