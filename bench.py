@@ -83,6 +83,16 @@ class Clocks:
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons}
 
 
+def measured_traffic(n):
+    """DRAM bytes per launch scaled from the committed ncu capture."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f)["scan_kernel<1, 1>"]
+        return int((t["dram_read"] + t["dram_write"]) * n / t["input_bytes"])
+    except Exception:
+        return None
+
+
 def make_input(size):
     from falx_gb300 import gen
 
@@ -295,7 +305,7 @@ def bench_gpu(args):
                    "bytes": n, "structurals": int(n_struct), "rows": int(rows), "tile_bytes": 16384,
                    "l2": "input 1 GiB > L2, no flush", "parallelism": "replicas" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                     "frac": round(achieved / peak, 4), "traffic": measured_traffic(n), "peak_kind": peak_kind,
                      "algorithmic_bytes": int(algo)},
         "cpu_baseline": cpu,
         "e2e": e2e,
