@@ -78,7 +78,11 @@ SIGNATURES = {
     "falx_index_structurals_host": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64,
                                             POINTER(c_uint64)]),
     "falx_parse_host": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, POINTER(falx_outputs)]),
+    "falx_index_structurals_noalloc": (c_int, [c_int, c_int, c_void_p, c_uint64, c_void_p, c_uint64,
+                                               POINTER(c_uint64), c_void_p]),
 }
+
+NOALLOC_MAX_BYTES = 256 << 20
 
 _lib = None
 

@@ -1477,3 +1477,136 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free structural index.
+//
+// Some callers cannot allocate device memory at all: code running under an
+// allocator that forbids it (a memory pool that is already full, a process
+// that must not grow its footprint while serving), plugins called from a
+// host that owns every allocation, or code paths that must not take the
+// driver's allocation locks. For them this entry point runs the same index
+// kernel as falx_index_structurals without a context: its look-back scratch
+// (one status record per 16 KiB tile plus a small header) lives in the
+// file-scope array below, reserved when the library is loaded. Every GPU
+// that loads the library holds those bytes until the process exits.
+// ===========================================================================
+namespace {
+
+constexpr uint64_t kNoAllocMaxBytes = FALX_NOALLOC_MAX_BYTES;
+// Tiles are cut on the buffer's 16-byte address grid, so a misaligned
+// buffer can span one tile more than len / kTile rounded up.
+constexpr uint32_t kNoAllocMaxTiles = (uint32_t)((kNoAllocMaxBytes + 15 + kTile - 1) / kTile) + 1;
+
+struct NoAllocScratch {
+    DevHeader hdr;
+    alignas(64) TileStatus status[kNoAllocMaxTiles];
+};
+
+struct NoAllocDevice {
+    bool ready;
+    NoAllocScratch *scratch;  // device address of g_noalloc_scratch on this device
+    int sm_count;
+    int blocks_per_sm[5];
+    uint32_t epoch;
+};
+
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+}  // namespace
+
+// The scratch itself. In host code this name is only a stand-in for the
+// symbol; the device address comes from cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+namespace {
+
+template <int D>
+int noalloc_setup_kernel(NoAllocDevice &dv) {
+    const void *fn = (const void *)index_kernel<D>;
+    FALX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemIx)));
+    int nb = 0;
+    FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, sizeof(SmemIx)));
+    dv.blocks_per_sm[D] = nb > 0 ? nb : 1;
+    return FALX_OK;
+}
+
+// Once per device, with that device current.
+int noalloc_setup(int device) {
+    NoAllocDevice &dv = g_noalloc_dev[device];
+    void *ptr = nullptr;
+    FALX_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+    FALX_CUDA(cudaDeviceGetAttribute(&dv.sm_count, cudaDevAttrMultiProcessorCount, device));
+    int rc = noalloc_setup_kernel<D_CSV>(dv);
+    if (!rc) rc = noalloc_setup_kernel<D_CSV_HASH>(dv);
+    if (!rc) rc = noalloc_setup_kernel<D_TSV>(dv);
+    if (!rc) rc = noalloc_setup_kernel<D_LOGFMT>(dv);
+    if (!rc) rc = noalloc_setup_kernel<D_NDJSON>(dv);
+    if (rc) return rc;
+    dv.scratch = static_cast<NoAllocScratch *>(ptr);
+    dv.epoch = 0;
+    dv.ready = true;
+    return FALX_OK;
+}
+
+int noalloc_run(int device, int dialect, const uint8_t *data, uint64_t len, uint32_t *out, uint64_t cap,
+                uint64_t *n_out, cudaStream_t stream) {
+    NoAllocDevice &dv = g_noalloc_dev[device];
+    if (!dv.ready) {
+        int rc = noalloc_setup(device);
+        if (rc) return rc;
+    }
+    // Status records are tagged with a launch epoch, so only the header must
+    // start at zero; the whole array is cleared when the epoch wraps.
+    if (++dv.epoch >= (1u << 28)) {
+        FALX_CUDA(cudaMemsetAsync(dv.scratch, 0, sizeof(NoAllocScratch), stream));
+        dv.epoch = 1;
+    }
+    FALX_CUDA(cudaMemsetAsync(&dv.scratch->hdr, 0, sizeof(DevHeader), stream));
+    Params P;
+    memset(&P, 0, sizeof P);
+    const uint64_t shift = (uint64_t)((uintptr_t)data & 15u);
+    P.data = data;
+    P.abase = data - shift;
+    P.len = len;
+    P.shift = (uint32_t)shift;
+    P.num_tiles = (uint32_t)((len + shift + kTile - 1) / kTile);
+    P.epoch = dv.epoch;
+    P.status = dv.scratch->status;
+    P.hdr = &dv.scratch->hdr;
+    P.index = cap ? out : nullptr;
+    P.index_cap = cap;
+    uint64_t grid = (uint64_t)dv.sm_count * (uint64_t)dv.blocks_per_sm[dialect];
+    if (grid > P.num_tiles) grid = P.num_tiles;
+    void *args[] = {(void *)&P};
+    const void *fn = dialect == FALX_CSV        ? (const void *)index_kernel<D_CSV>
+                     : dialect == FALX_CSV_HASH ? (const void *)index_kernel<D_CSV_HASH>
+                     : dialect == FALX_TSV      ? (const void *)index_kernel<D_TSV>
+                     : dialect == FALX_LOGFMT   ? (const void *)index_kernel<D_LOGFMT>
+                                                : (const void *)index_kernel<D_NDJSON>;
+    FALX_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(kThreads), args, sizeof(SmemIx), stream));
+    DevHeader h;
+    FALX_CUDA(cudaMemcpyAsync(&h, &dv.scratch->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, stream));
+    FALX_CUDA(cudaStreamSynchronize(stream));
+    *n_out = h.n_struct;
+    if (h.error) return FALX_ERR_TIMEOUT;
+    return h.n_struct > cap ? FALX_ERR_CAPACITY : FALX_OK;
+}
+
+}  // namespace
+
+extern "C" int falx_index_structurals_noalloc(int device, int dialect, const uint8_t *data, uint64_t len,
+                                              uint32_t *out, uint64_t cap, uint64_t *n_out, void *stream) {
+    if (!n_out || !valid_dialect(dialect) || device < 0 || device >= kNoAllocMaxDevices) return FALX_ERR_INVALID;
+    if ((len && !data) || (cap && !out)) return FALX_ERR_INVALID;
+    *n_out = 0;
+    if (len > kNoAllocMaxBytes) return FALX_ERR_INPUT_TOO_LARGE;
+    if (len == 0) return FALX_OK;
+    int prev = 0;
+    FALX_CUDA(cudaGetDevice(&prev));
+    if (prev != device) FALX_CUDA(cudaSetDevice(device));
+    const int rc = noalloc_run(device, dialect, data, len, out, cap, n_out, (cudaStream_t)stream);
+    if (prev != device) cudaSetDevice(prev);
+    return rc;
+}

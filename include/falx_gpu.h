@@ -181,6 +181,23 @@ int falx_index_structurals_host(falx_ctx *ctx, int dialect, const uint8_t *host_
 int falx_parse_host(falx_ctx *ctx, const falx_schema *schema, const uint8_t *host_data, uint64_t len,
                     falx_outputs *host_out);
 
+/* Structural index without any allocation (no counterpart in the
+ * reference, whose callers are Rust code that allocates freely). For callers
+ * that may not allocate device memory: the look-back scratch is a fixed
+ * array inside the library (about 1 MiB per GPU that loads it, held until the
+ * process exits), so inputs are limited to FALX_NOALLOC_MAX_BYTES
+ * (FALX_ERR_INPUT_TOO_LARGE beyond). `data` and `out` are device pointers in
+ * `device`; `stream` is a cudaStream_t (NULL = legacy default stream); the
+ * call returns after the stream has drained. The first call on a device also
+ * sets that device up (looks up the scratch address, sets kernel
+ * attributes), so make it before any stream capture. All calls share the
+ * one scratch array: calls whose work can overlap on a GPU (other host
+ * threads, other streams) race and must be serialised by the caller.
+ * Output is identical to falx_index_structurals. */
+#define FALX_NOALLOC_MAX_BYTES (256ull << 20)
+int falx_index_structurals_noalloc(int device, int dialect, const uint8_t *data, uint64_t len, uint32_t *out,
+                                   uint64_t cap, uint64_t *n_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
