@@ -193,6 +193,43 @@ class Engine:
             check(rc, "falx_parse_columns")
             return Columns(schema, cols.rows, bufs, [cols.cols[k].str_len for k in range(len(schema.columns))], d)
 
+    def parse_all(self, data, schema, stats_fields=(4, 5)):
+        """Every output of one fused falx_parse pass: structural index, tape,
+        columns, field-byte counts and count/sum stats."""
+        torch = self.torch
+        d = self.to_device(data)
+        n = d.numel()
+        self._sync_stream()
+        cs = schema.to_c()
+        icap, scap, ecap = n // 4 + 64, n // 4 + 64, n // 8 + 64
+        rows_cap, str_cap = n // 8 + 64, n + 64
+        while True:
+            index = self.empty(icap, torch.int32)
+            seps = self.empty(scap, torch.int32)
+            ends = self.empty(ecap, torch.int64)
+            bufs = self.alloc_columns(schema, rows_cap, str_cap)
+            cols = self.columns_struct(schema, bufs, rows_cap, str_cap)
+            fb = _lib.falx_field_byte_stats()
+            st = _lib.falx_geo_stats()
+            out = _lib.falx_outputs()
+            out.index, out.index_cap = index.data_ptr(), icap
+            out.seps, out.seps_cap = seps.data_ptr(), scap
+            out.ends, out.ends_cap = ends.data_ptr(), ecap
+            out.columns = ctypes.pointer(cols)
+            out.field_bytes = ctypes.pointer(fb)
+            out.stats = ctypes.pointer(st)
+            out.stats_fields[0], out.stats_fields[1] = stats_fields
+            rc = self.lib.falx_parse(self.ctx, byref(cs), c_void_p(d.data_ptr()), n, byref(out))
+            if rc == _lib.FALX_ERR_CAPACITY:
+                icap, scap, ecap = max(icap, out.n_index), max(scap, out.n_seps), max(ecap, out.n_ends)
+                rows_cap = max(rows_cap, cols.rows)
+                str_cap = max([str_cap] + [cols.cols[k].str_len for k in range(len(schema.columns))])
+                continue
+            check(rc, "falx_parse")
+            columns = Columns(schema, cols.rows, bufs, [cols.cols[k].str_len for k in range(len(schema.columns))], d)
+            return {"index": index[: out.n_index], "seps": seps[: out.n_seps], "ends": ends[: out.n_ends],
+                    "columns": columns, "field_bytes": FieldByteStats(fb.fields, fb.bytes), "stats": GeoStats(st)}
+
     def stats_count_sum(self, data, dialect, field0, field1):
         d = self.to_device(data)
         self._sync_stream()

@@ -89,14 +89,6 @@ struct Params {
 };
 
 // Shared state of the block-wide look-back.
-struct LookbackShared {
-    uint32_t wf[kWarps];
-    uint64_t wc[kWarps][4];
-    uint32_t nearest;
-    uint32_t stop;
-    uint32_t entry;
-    uint32_t pre[3];
-};
 
 // Shared-memory layout (dynamic).
 template <bool ROWS>
@@ -104,12 +96,11 @@ struct Smem {
     static constexpr int kHalo = ROWS ? kHaloBytes : 0;
     static constexpr int kBuf = kPre + kTile + kHalo;  // multiple of 16
     alignas(128) uint8_t buf[2][kBuf];
-    uint16_t stage[kTile + kHalo];
+    uint16_t stage[ROWS ? kStageCap + kHalo : kTile];
     uint64_t bar[2];
     uint32_t warp_f[kWarps];
     unsigned long long warp_c[kWarps];
     unsigned long long warp_agg[kWarps][4];
-    LookbackShared lb;
     uint32_t entry_state;
     uint32_t tile_f;
     uint32_t base[3];       // global structural / terminator / row offsets of the tile
@@ -477,7 +468,7 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uin
         while (mm) {
             unsigned bpos = __ffsll((long long)mm) - 1;
             uint32_t rel = (uint32_t)(tid * kThreadBytes + bpos);
-            if (k < (uint32_t)kTile) S.stage[k] = (uint16_t)(rel | (((term >> bpos) & 1) << 15));
+            if (k < (uint32_t)(ROWS ? kStageCap : kTile)) S.stage[k] = (uint16_t)(rel | (((term >> bpos) & 1) << 15));
             k++;
             mm &= mm - 1;
         }
@@ -485,12 +476,23 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uin
     __syncthreads();
     const uint32_t n_tile = cfield(S.tile_c, 0);
     const uint32_t sbase = S.base[0];
+    const bool overflow = ROWS && n_tile > (uint32_t)kStageCap;
 
-    // ---- structural index, coalesced
-    if (p.index) {
+    // ---- structural index: coalesced from the staging list, or straight
+    // from the masks when the tile is too dense to stage
+    if (p.index && !overflow) {
         for (uint32_t i = tid; i < n_tile; i += kThreads) {
             uint64_t g = (uint64_t)sbase + i;
             if (g < p.index_cap) p.index[g] = (uint32_t)(vs + (S.stage[i] & 0x7FFF));
+        }
+    } else if (p.index) {
+        uint64_t g = (uint64_t)sbase + cfield(ce, 0);
+        uint64_t mm = stm;
+        while (mm) {
+            const unsigned bpos = __ffsll((long long)mm) - 1;
+            if (g < p.index_cap) p.index[g] = (uint32_t)(base_t + bpos);
+            g++;
+            mm &= mm - 1;
         }
     }
     // ---- tape: separators and record ends
@@ -536,7 +538,7 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS> &S, uin
         // does the tile's first byte start a record (comment records included)?
         const bool rec0 = vs <= 0 || (b[kPre - 1] == '\n' && state_outside<D>(entry));
         rows_phase<D>(p.rows, rc, S.rs, S.stage, rows_m, stm, term, cfield(ce, 0), cfield(ce, 1), cfield(ce, 2),
-                      cfield(S.tile_c, 1), cfield(S.tile_c, 2), rec0, base_t, tid);
+                      cfield(S.tile_c, 1), cfield(S.tile_c, 2), rec0, overflow, base_t, tid);
     }
 }
 

@@ -19,10 +19,11 @@ namespace falx {
 constexpr int kMaxStr = 4;          // string columns with an arena per call
 constexpr int kHaloBytes = 1024;    // bytes staged after each tile
 constexpr int kMaxCols = 32;
-constexpr int kLocalRows = 2048;    // rows per tile with shared-memory validity staging
+constexpr int kLocalRows = 1024;    // rows per tile with shared-memory validity staging
 constexpr int kVWords = kLocalRows / 64 + 2;
 constexpr int kRowCap = kLocalRows; // rows per tile on the data-parallel path
-constexpr int kTermCap = 4096;      // terminators per tile (+ halo) on the data-parallel path
+constexpr int kTermCap = 2048;      // terminators per tile (+ halo) on the data-parallel path
+constexpr int kStageCap = 4096;     // staged structurals of the tile itself (the halo adds up to kHaloBytes)
 
 struct RowSpec {
     int ncols;
@@ -549,7 +550,7 @@ template <int D>
 __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> &sh, uint16_t *stage,
                            uint64_t rows_m, uint64_t stm, uint64_t term, uint32_t excl_struct, uint32_t excl_term,
                            uint32_t excl_rows, uint32_t nterm_tile, uint32_t nrows_tile, bool tile_rec0,
-                           int64_t base_t, int tid) {
+                           bool overflow, int64_t base_t, int tid) {
     const int lane = tid & 31, warp = tid >> 5;
     const int64_t ve = rc.vs + kTile;
 
@@ -568,7 +569,7 @@ __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> 
     for (int i = tid; i < rs.ncols * kVWords; i += kThreads) sh.vbits[i / kVWords][i % kVWords] = 0;
 
     // ---- row and terminator tables for the data-parallel path
-    const bool tables = nrows_tile <= (uint32_t)kRowCap && nterm_tile < (uint32_t)kTermCap;
+    const bool tables = !overflow && nrows_tile <= (uint32_t)kRowCap && nterm_tile < (uint32_t)kTermCap;
     if (tables) {
         uint64_t mm = rows_m;
         uint32_t r = excl_rows;
@@ -593,7 +594,7 @@ __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> 
     // ---- halo: structurals after the tile up to the first terminator
     if (warp == 0) {
         uint32_t n_halo = 0, kind = 1, hexit = rc.exit_state;
-        if (ve < rc.len) {
+        if (ve < rc.len && !overflow) {
             Masks m;
             m.s = m.nl = m.q = m.x = 0;
             m.special = false;
@@ -691,7 +692,10 @@ __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> 
         const int64_t r0 = base_t + b;
         const uint64_t g = (uint64_t)rc.row_base + lr;
         wk.k = excl_struct + __popcll(stm & ((1ull << b) - 1));
-        wk.serial = false;
+        wk.serial = overflow;  // tiles too dense to stage walk their records byte by byte
+        wk.sp = r0;
+        wk.ss = 0;
+        wk.sls = true;
         uint32_t done = 0;  // columns written
         int64_t fs = r0;
         uint32_t ord = 0;
@@ -891,7 +895,10 @@ __device__ void rows_phase(const RowSpec &rs, const RowCtx &rc, RowShared<true> 
             const int64_t r0 = base_t + b;
             const uint64_t g = (uint64_t)rc.row_base + lr;
             wk.k = excl_struct + __popcll(stm & ((1ull << b) - 1));
-            wk.serial = false;
+            wk.serial = overflow;
+            wk.sp = r0;
+            wk.ss = 0;
+            wk.sls = true;
             int64_t fs = r0;
             uint32_t ord = 0;
             for (;;) {

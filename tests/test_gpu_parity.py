@@ -231,3 +231,67 @@ def test_ndjson_generated(engine):
     assert st.sum_score_e6 == want["sum_score_e6"]
     assert st.total_e6 == want["total_e6"]
     assert st.total_f64 == want["total_f64"]
+
+
+def dense_mixed_doc(rng, dialect, size):
+    """Stretches of very short fields (more structurals per 16 KiB tile than
+    the row kernel stages) between stretches of ordinary rows."""
+    sep = {fx.CSV: b",", fx.CSV_HASH: b",", fx.TSV: b"\t", fx.LOGFMT: b" "}[dialect]
+    out = bytearray()
+    while len(out) < size:
+        if (len(out) // 40_000) % 2 == 0:
+            for _ in range(2000):
+                nf = 1 + rng.next() % 6
+                cells = []
+                for _ in range(nf):
+                    k = rng.next() % 6
+                    cells.append([b"", b"1", b"-2", b"a", b"3.5", b'""'][k] if dialect != fx.TSV
+                                 else [b"", b"1", b"-2", b"a", b"3.5", b"x"][k])
+                out += sep.join(cells) + (b"\r\n" if rng.next() % 9 == 0 else b"\n")
+                if dialect == fx.CSV_HASH and rng.next() % 17 == 0:
+                    out += b"#c,1\n"
+        else:
+            for _ in range(300):
+                out += sep.join([b"%d" % (rng.next() % 100000), b"name%d" % (rng.next() % 97),
+                                 b"%d.%06d" % (rng.next() % 90, rng.next() % 10**6),
+                                 b"%d" % (rng.next() % 7), b"-%d.25" % (rng.next() % 180), b"%d.5" % (rng.next() % 90)])
+                out += b"\n"
+    return bytes(out[:size])
+
+
+FUSED_COLS = [(0, fx.I64), (1, fx.STR), (2, fx.F64), (3, fx.U32), (4, fx.BYTES), (5, fx.STR)]
+
+
+@pytest.mark.parametrize("dialect", [fx.CSV, fx.CSV_HASH, fx.TSV, fx.LOGFMT])
+def test_fused_parse_dense_and_ordinary_tiles(engine, dialect):
+    # One falx_parse pass with every output requested, checked output by
+    # output against the oracle.
+    rng = Rng(0xF00D + dialect)
+    doc = dense_mixed_doc(rng, dialect, 3 << 20)
+    got = engine.parse_all(doc, fx.Schema(dialect, FUSED_COLS), stats_fields=(2, 5))
+    assert np.array_equal(got["index"].cpu().numpy().view(np.uint32), oracle.index_spec(doc, dialect))
+    ws, we = oracle.parse_tape(doc, dialect)
+    assert np.array_equal(got["seps"].cpu().numpy().view(np.uint32), ws)
+    assert np.array_equal(got["ends"].cpu().numpy().view(np.uint64), we)
+    rows, want = oracle.parse_columns(doc, dialect, FUSED_COLS)
+    compare_columns(got["columns"], rows, want, FUSED_COLS)
+    fb = got["field_bytes"]
+    assert (fb.fields, fb.bytes) == oracle.field_bytes(doc, dialect)
+    st, ws = got["stats"], oracle.geo_stats(doc, dialect, 2, 5)
+    assert st.records == ws.records and st.values == tuple(ws.values) and st.checksum == tuple(ws.checksum)
+    assert st.sum_e6 == tuple(ws.sum_e6) and st.inexact == tuple(ws.inexact)
+
+
+@pytest.mark.parametrize("kind,dialect", [(gen.CSV_HASH, fx.CSV_HASH), (gen.ADVERSARIAL, fx.CSV_HASH),
+                                          (gen.CSV_GEO, fx.CSV)])
+def test_fused_parse_generated(engine, kind, dialect):
+    doc = gen.generate(kind, 5 << 20)
+    got = engine.parse_all(doc, fx.Schema(dialect, GEO_COLS))
+    assert np.array_equal(got["index"].cpu().numpy().view(np.uint32), oracle.index_spec(doc, dialect))
+    ws, we = oracle.parse_tape(doc, dialect)
+    assert np.array_equal(got["seps"].cpu().numpy().view(np.uint32), ws)
+    assert np.array_equal(got["ends"].cpu().numpy().view(np.uint64), we)
+    rows, want = oracle.parse_columns(doc, dialect, GEO_COLS)
+    compare_columns(got["columns"], rows, want, GEO_COLS)
+    fb = got["field_bytes"]
+    assert (fb.fields, fb.bytes) == oracle.field_bytes(doc, dialect)
