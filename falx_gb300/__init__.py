@@ -230,6 +230,63 @@ class Engine:
             return {"index": index[: out.n_index], "seps": seps[: out.n_seps], "ends": ends[: out.n_ends],
                     "columns": columns, "field_bytes": FieldByteStats(fb.fields, fb.bytes), "stats": GeoStats(st)}
 
+    # ---- learned speculation -------------------------------------------
+    def model_create(self, seed=1):
+        """A freshly initialised entry-region predictor on this engine's GPU."""
+        return EntryModel(self, seed)
+
+    def region_states(self, data, dialect):
+        """Exact region state at the start of every 64-byte block (labels)."""
+        torch = self.torch
+        d = self.to_device(data)
+        self._sync_stream()
+        n = c_uint64()
+        self.lib.falx_region_states(self.ctx, dialect, c_void_p(d.data_ptr()), d.numel(), None, 0, byref(n))
+        out = self.empty(max(n.value, 1), torch.uint8)
+        check(self.lib.falx_region_states(self.ctx, dialect, c_void_p(d.data_ptr()), d.numel(),
+                                          c_void_p(out.data_ptr()), n.value, byref(n)), "falx_region_states")
+        return out[: n.value]
+
+    def byte_classes(self, data, starts):
+        """Classes of the 256 bytes from each start offset: uint8 [n, 256]."""
+        torch = self.torch
+        d = self.to_device(data)
+        st = starts.to(device=d.device, dtype=torch.int64).contiguous()
+        self._sync_stream()
+        n = st.numel()
+        cls = self.empty(max(n, 1) * _lib.MLP_BYTES, torch.uint8)
+        check(self.lib.falx_byte_classes(self.ctx, c_void_p(d.data_ptr()), d.numel(), c_void_p(st.data_ptr()), n,
+                                         c_void_p(cls.data_ptr())), "falx_byte_classes")
+        return cls[: n * _lib.MLP_BYTES].view(n, _lib.MLP_BYTES)
+
+    def index_structurals_speculative(self, data, dialect, model=None, assumed=None):
+        """Speculative structural index: (index, tiles, mispredicted). Entry
+        states come from `model`, from the per-tile array `assumed`, or (both
+        None) are taken as the file's initial state."""
+        torch = self.torch
+        d = self.to_device(data)
+        self._sync_stream()
+        n = d.numel()
+        cap = n // 4 + 64
+        st = _lib.falx_spec_stats()
+        while True:
+            out = self.empty(cap, torch.int32)
+            cnt = c_uint64()
+            if assumed is not None:
+                a = assumed.to(device=d.device, dtype=torch.uint8).contiguous()
+                rc = self.lib.falx_index_structurals_assumed(self.ctx, dialect, c_void_p(d.data_ptr()), n,
+                                                             c_void_p(a.data_ptr()), c_void_p(out.data_ptr()), cap,
+                                                             byref(cnt), byref(st))
+            else:
+                rc = self.lib.falx_index_structurals_speculative(self.ctx, model.ptr if model else None, dialect,
+                                                                 c_void_p(d.data_ptr()), n, c_void_p(out.data_ptr()),
+                                                                 cap, byref(cnt), byref(st))
+            if rc == _lib.FALX_ERR_CAPACITY and cnt.value > cap:
+                cap = cnt.value
+                continue
+            check(rc, "falx_index_structurals_speculative")
+            return out[: cnt.value], st.tiles, st.mispredicted
+
     def stats_count_sum(self, data, dialect, field0, field1):
         d = self.to_device(data)
         self._sync_stream()
@@ -253,6 +310,88 @@ class Engine:
         check(self.lib.falx_ndjson_id_score(self.ctx, c_void_p(d.data_ptr()), d.numel(), byref(st)),
               "falx_ndjson_id_score")
         return NdjsonIdScoreStats(st)
+
+
+class EntryModel:
+    """Entry-region predictor (falx_model): 256 leading bytes of a tile ->
+    NORMAL / QUOTE / COMMENT. Trained and run by the engine's own kernels."""
+
+    def __init__(self, engine, seed=1):
+        self.engine = engine
+        p = c_void_p()
+        check(engine.lib.falx_model_create(engine.ctx, seed, byref(p)), "falx_model_create")
+        self.ptr = p
+
+    def close(self):
+        if self.ptr:
+            self.engine.lib.falx_model_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_confidence(self, min_prob):
+        """Tiles predicted with probability below min_prob assume nothing."""
+        check(self.engine.lib.falx_model_set_confidence(self.ptr, min_prob), "falx_model_set_confidence")
+
+    @staticmethod
+    def param_count():
+        return int(_lib.load().falx_model_param_count())
+
+    def get(self):
+        w = np.empty(self.param_count(), dtype=np.float32)
+        check(self.engine.lib.falx_model_get(self.engine.ctx, self.ptr, c_void_p(w.ctypes.data), w.size),
+              "falx_model_get")
+        return w
+
+    def set(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        check(self.engine.lib.falx_model_set(self.engine.ctx, self.ptr, c_void_p(w.ctypes.data), w.size),
+              "falx_model_set")
+
+    def forward(self, cls):
+        """Logits [n, 3] (float32) and the predicted states [n] (uint8)."""
+        torch = self.engine.torch
+        cls = cls.contiguous()
+        n = cls.shape[0]
+        z = self.engine.empty(max(n, 1) * 3, torch.float32)
+        pred = self.engine.empty(max(n, 1), torch.uint8)
+        check(self.engine.lib.falx_model_forward(self.engine.ctx, self.ptr, c_void_p(cls.data_ptr()), n,
+                                                 c_void_p(z.data_ptr()), c_void_p(pred.data_ptr())),
+              "falx_model_forward")
+        return z[: n * 3].view(n, 3), pred[:n]
+
+    def grad(self, cls, labels):
+        """Gradient of the mean cross-entropy (flat float32, parameter order
+        of falx_model_get) and the loss."""
+        torch = self.engine.torch
+        g = self.engine.empty(self.param_count(), torch.float32)
+        loss = ctypes.c_float()
+        check(self.engine.lib.falx_model_grad(self.engine.ctx, self.ptr, c_void_p(cls.contiguous().data_ptr()),
+                                              c_void_p(labels.contiguous().data_ptr()), cls.shape[0],
+                                              c_void_p(g.data_ptr()), byref(loss)), "falx_model_grad")
+        return g, loss.value
+
+    def train(self, cls, labels, batch=512, epochs=1, lr=1e-3):
+        loss = ctypes.c_float()
+        check(self.engine.lib.falx_model_train(self.engine.ctx, self.ptr, c_void_p(cls.contiguous().data_ptr()),
+                                               c_void_p(labels.contiguous().data_ptr()), cls.shape[0], batch, epochs,
+                                               lr, byref(loss)), "falx_model_train")
+        return loss.value
+
+    def predict_tiles(self, data):
+        torch = self.engine.torch
+        d = self.engine.to_device(data)
+        self.engine._sync_stream()
+        tiles = (d.numel() + (d.data_ptr() & 15) + _lib.SPEC_TILE - 1) // _lib.SPEC_TILE
+        out = self.engine.empty(max(tiles, 1), torch.uint8)
+        n = c_uint64()
+        check(self.engine.lib.falx_predict_tiles(self.engine.ctx, self.ptr, c_void_p(d.data_ptr()), d.numel(),
+                                                 c_void_p(out.data_ptr()), tiles, byref(n)), "falx_predict_tiles")
+        return out[: n.value]
 
 
 class GeoStats:

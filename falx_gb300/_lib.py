@@ -3,7 +3,8 @@ library is missing: there is no CPU fallback."""
 
 import ctypes
 import os
-from ctypes import POINTER, Structure, c_char_p, c_double, c_int, c_int32, c_int64, c_uint32, c_uint64, c_void_p
+from ctypes import (POINTER, Structure, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_uint32, c_uint64,
+                    c_void_p)
 
 from . import build
 
@@ -60,6 +61,10 @@ class falx_ndjson_stats(Structure):
                 ("total_e6_lo", c_int64), ("total_e6_hi", c_int64), ("total_f64", c_double)]
 
 
+class falx_spec_stats(Structure):
+    _fields_ = [("tiles", c_uint64), ("mispredicted", c_uint64)]
+
+
 # Every symbol the header declares, with its signature.
 SIGNATURES = {
     "falx_create": (c_int, [c_int, POINTER(c_void_p)]),
@@ -80,7 +85,27 @@ SIGNATURES = {
     "falx_parse_host": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, POINTER(falx_outputs)]),
     "falx_index_structurals_noalloc": (c_int, [c_int, c_int, c_void_p, c_uint64, c_void_p, c_uint64,
                                                POINTER(c_uint64), c_void_p]),
+    "falx_model_param_count": (c_uint64, []),
+    "falx_model_create": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
+    "falx_model_destroy": (None, [c_void_p]),
+    "falx_model_set_confidence": (c_int, [c_void_p, c_float]),
+    "falx_model_get": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64]),
+    "falx_model_set": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64]),
+    "falx_byte_classes": (c_int, [c_void_p, c_void_p, c_uint64, c_void_p, c_uint32, c_void_p]),
+    "falx_model_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p]),
+    "falx_model_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, POINTER(c_float)]),
+    "falx_model_train": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64, c_uint32, c_uint32, c_float,
+                                 POINTER(c_float)]),
+    "falx_region_states": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64)]),
+    "falx_predict_tiles": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64)]),
+    "falx_index_structurals_assumed": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_void_p, c_uint64,
+                                               POINTER(c_uint64), POINTER(falx_spec_stats)]),
+    "falx_index_structurals_speculative": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_uint64, c_void_p,
+                                                   c_uint64, POINTER(c_uint64), POINTER(falx_spec_stats)]),
 }
+
+MLP_BYTES = 256
+SPEC_TILE = 16384
 
 NOALLOC_MAX_BYTES = 256 << 20
 

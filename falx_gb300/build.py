@@ -15,7 +15,7 @@ GEN_LIB = os.path.join(PKG, "libfalx_gen.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 GPU_SOURCES = ["falx_gpu.cu"]
-GPU_DEPS = ["scan_core.cuh", "rows.cuh", "decimal.cuh", "pow5_table.h", "ndjson.cuh"]
+GPU_DEPS = ["scan_core.cuh", "rows.cuh", "decimal.cuh", "pow5_table.h", "ndjson.cuh", "mlp.cuh"]
 
 
 def _nvcc():

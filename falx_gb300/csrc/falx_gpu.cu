@@ -26,6 +26,7 @@
 #include <new>
 
 #include "../../include/falx_gpu.h"
+#include "mlp.cuh"
 #include "ndjson.cuh"
 #include "rows.cuh"
 #include "scan_core.cuh"
@@ -64,6 +65,7 @@ struct DevHeader {
     unsigned long long arena[kMaxStr];
     unsigned long long fb_fields, fb_bytes;
     unsigned long long st_records, st_values[2], st_checksum[2], st_sum_e6[2], st_inexact[2];
+    unsigned long long spec_repairs;  // speculative tiles whose assumed entry state was wrong
 };
 
 enum : uint32_t { ERR_TIMEOUT = 1, ERR_ARENA = 2, ERR_TMA = 4 };
@@ -85,6 +87,8 @@ struct Params {
     uint64_t seps_cap;
     uint64_t *ends;
     uint64_t ends_cap;
+    const uint8_t *pred;   // speculative index: assumed entry state of every tile
+    uint8_t *states64;     // optional: entry state of every 64-byte block
     RowSpec rows;
 };
 
@@ -224,6 +228,62 @@ __device__ __forceinline__ void agg_prepend(uint32_t gf, const uint64_t (&gc)[4]
     f = fcompose(gf, f);
 }
 
+// Counts packed 21 bits apart hold one tile (at most 16384 each); sums over
+// longer spans are kept unpacked. In speculative aggregates bit 63 marks
+// counts that are not known (entry states the tile did not assume).
+constexpr uint64_t kUnknown = 1ull << 63;
+// Assumed entry of a speculative tile that counted under every entry state.
+constexpr uint32_t kAllStates = 0xFF;
+
+// Transfer function that sends every state to x.
+__device__ __forceinline__ uint32_t fconst(uint32_t x) { return x * 0x55u; }
+
+// Prepend an older packed aggregate (gf, gc) of at most 128 tiles to a wide
+// one (f, c, unknown-state mask u): (f . gf, gc[s] + c[gf(s)]).
+template <int NS>
+__device__ __forceinline__ void wide_prepend(uint32_t gf, const unsigned long long (&gc)[4], uint32_t &f,
+                                             uint32_t (&c)[4][3], uint32_t &u) {
+    uint32_t r[4][3], ru = 0;
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+        const uint32_t m = fapply(gf, s);
+        uint32_t c0 = c[0][0], c1 = c[0][1], c2 = c[0][2];
+#pragma unroll
+        for (int t = 1; t < NS; t++)
+            if (m == (uint32_t)t) { c0 = c[t][0]; c1 = c[t][1]; c2 = c[t][2]; }
+        r[s][0] = cfield(gc[s], 0) + c0;
+        r[s][1] = cfield(gc[s], 1) + c1;
+        r[s][2] = cfield(gc[s], 2) + c2;
+        ru |= (((uint32_t)(gc[s] >> 63) | (u >> m)) & 1u) << s;
+    }
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+        c[s][0] = r[s][0];
+        c[s][1] = r[s][1];
+        c[s][2] = r[s][2];
+    }
+    u = ru;
+    f = fcompose(gf, f);
+}
+
+// As agg_prepend, keeping the unknown mark (speculative aggregates).
+template <int NS>
+__device__ __forceinline__ void agg_prepend_spec(uint32_t gf, const uint64_t (&gc)[4], uint32_t &f,
+                                                 uint64_t (&c)[4]) {
+    uint64_t r[4];
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+        const uint32_t m = fapply(gf, s);
+        uint64_t cm = c[0];
+#pragma unroll
+        for (int t = 1; t < NS; t++) cm = m == (uint32_t)t ? c[t] : cm;
+        r[s] = (((gc[s] & ~kUnknown) + (cm & ~kUnknown)) | ((gc[s] | cm) & kUnknown));
+    }
+#pragma unroll
+    for (int s = 0; s < NS; s++) c[s] = r[s];
+    f = fcompose(gf, f);
+}
+
 // Decoupled look-back over (transfer function, counts per entry state)
 // aggregates, run by one warp: lane l watches predecessor hi - l. A probe
 // ends as soon as every predecessor nearer than the nearest published
@@ -235,7 +295,8 @@ __device__ __forceinline__ void agg_prepend(uint32_t gf, const uint64_t (&gc)[4]
 template <int NS>
 __device__ uint32_t lookback(const Params &p, uint32_t tile, int lane, uint32_t pre[3]) {
     uint32_t af = kIdentity;  // aggregate of the tiles between the window and `tile`
-    uint64_t ac[4] = {0, 0, 0, 0};
+    uint32_t ac[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    uint32_t au = 0;
     const uint64_t t0 = globaltimer_ns();
     for (int64_t hi = (int64_t)tile - 1; hi >= 0; hi -= 32) {
         const int64_t j = hi - lane;
@@ -276,10 +337,10 @@ __device__ uint32_t lookback(const Params &p, uint32_t tile, int lane, uint32_t 
             if (lane + d < 32) agg_prepend<NS>(gf, gc, f, c);  // lane + d covers older tiles
         }
         uint32_t wf = __shfl_sync(0xffffffffu, f, 0);
-        uint64_t wc[4];
+        unsigned long long wc[4];
 #pragma unroll
         for (int s = 0; s < NS; s++) wc[s] = __shfl_sync(0xffffffffu, c[s], 0);
-        agg_prepend<NS>(wf, wc, af, ac);
+        wide_prepend<NS>(wf, wc, af, ac, au);
         if (ball_incl) {
             uint32_t ex = 0, i0 = 0, i1 = 0, i2 = 0;
             if (lane == sidx) {
@@ -289,19 +350,20 @@ __device__ uint32_t lookback(const Params &p, uint32_t tile, int lane, uint32_t 
                 i2 = ld_relaxed(&p.status[j].incl[2]);
             }
             ex = __shfl_sync(0xffffffffu, ex, sidx);
-            uint64_t cc = ac[0];
+            uint32_t c0 = ac[0][0], c1 = ac[0][1], c2 = ac[0][2];
 #pragma unroll
-            for (int t = 1; t < NS; t++) cc = ex == (uint32_t)t ? ac[t] : cc;
-            pre[0] = __shfl_sync(0xffffffffu, i0, sidx) + cfield(cc, 0);
-            pre[1] = __shfl_sync(0xffffffffu, i1, sidx) + cfield(cc, 1);
-            pre[2] = __shfl_sync(0xffffffffu, i2, sidx) + cfield(cc, 2);
+            for (int t = 1; t < NS; t++)
+                if (ex == (uint32_t)t) { c0 = ac[t][0]; c1 = ac[t][1]; c2 = ac[t][2]; }
+            pre[0] = __shfl_sync(0xffffffffu, i0, sidx) + c0;
+            pre[1] = __shfl_sync(0xffffffffu, i1, sidx) + c1;
+            pre[2] = __shfl_sync(0xffffffffu, i2, sidx) + c2;
             return fapply(af, ex);
         }
     }
     // reached the first tile: the file starts outside every region
-    pre[0] = cfield(ac[0], 0);
-    pre[1] = cfield(ac[0], 1);
-    pre[2] = cfield(ac[0], 2);
+    pre[0] = ac[0][0];
+    pre[1] = ac[0][1];
+    pre[2] = ac[0][2];
     return fapply(af, 0);
 }
 
@@ -559,6 +621,7 @@ struct LocalState {
     uint32_t excl;
     bool prev_nl;
     unsigned long long cv[4];
+    uint64_t stm;  // speculative: structural mask under the assumed entry
 };
 
 struct SmemIx {
@@ -576,11 +639,18 @@ struct SmemIx {
     uint32_t lb_first_incl[3], lb_first_wait[3], lb_stop, lb_entry, lb_pre[3];
     uint32_t base[3];
     unsigned long long tile_c;
+    // speculative index: entry state assumed by the tile in its local pass
+    // and by the deferred one; counts of the look-back not known yet
+    uint32_t spec_p, pspec_p;
+    uint32_t lb_restart;
 };
 
 // Local pass of one tile: classify, scan transfer functions, publish the
 // aggregate. Leaves the per-thread state needed by the deferred output.
-template <int D>
+// SPEC: the tile assumes the entry state p.pred[tile] (tile 0 assumes the
+// file's initial state), counts only under that assumption and publishes
+// its full transfer function, the assumed entry and those counts.
+template <int D, bool SPEC>
 __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t tile, uint8_t *b, LocalState &L) {
     constexpr int kBuf = kPre + kTile;
     constexpr int NS = NStates<D>::value;
@@ -612,8 +682,10 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
     if (lane == 31) S.warp_f[warp] = incl;
     uint32_t excl = __shfl_up_sync(0xffffffffu, incl, 1);
     if (lane == 0) excl = kIdentity;
+    if (!SPEC) {
 #pragma unroll
-    for (int e = 0; e < NS; e++) L.cv[e] = thread_counts<D, false>(L.m, L.ls, L.prev_nl, e, L.base_t, len);
+        for (int e = 0; e < NS; e++) L.cv[e] = thread_counts<D, false>(L.m, L.ls, L.prev_nl, e, L.base_t, len);
+    }
     __syncthreads();
     if (warp == 0) {
         const uint32_t wf = lane < kWarps ? S.warp_f[lane] : kIdentity;
@@ -625,6 +697,38 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
     }
     __syncthreads();
     L.excl = fcompose(S.warp_f[warp], excl);
+    uint32_t pk = kAllStates;
+    if (SPEC) {
+        pk = (tile == 0 || !p.pred) ? 0u : (uint32_t)p.pred[tile];
+        if (pk >= (uint32_t)NS && pk != kAllStates) pk = 0;
+    }
+    if (SPEC && pk == kAllStates) {
+        // no assumption: count under every entry state, as the plain scan does
+#pragma unroll
+        for (int e = 0; e < NS; e++) L.cv[e] = thread_counts<D, false>(L.m, L.ls, L.prev_nl, e, L.base_t, len);
+    }
+    if (SPEC && pk != kAllStates) {
+        const uint32_t s_in = fapply(L.excl, pk);
+        L.stm = structural_mask<D>(L.m, L.ls, s_in);
+        unsigned long long v = (unsigned long long)__popcll(L.stm) |
+                               ((unsigned long long)__popcll(L.stm & L.m.nl) << 21);
+        L.cv[0] = v;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+        if (lane == 0) S.warp_agg[warp][0] = v;
+        __syncthreads();
+        if (tid == 0) {
+            TileStatus *tst = &p.status[tile];
+            unsigned long long agg = 0;
+            for (int w2 = 0; w2 < kWarps; w2++) agg += S.warp_agg[w2][0];
+            tst->func = S.tile_f | (pk << 8);
+            tst->agg[0] = agg;
+            st_release(&tst->flag, p.epoch * 4 + 1);
+            S.agg[0] = agg;
+            S.spec_p = pk;
+        }
+        return;
+    }
     {
         unsigned long long v[NS];
 #pragma unroll
@@ -649,23 +753,38 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
 #pragma unroll
         for (int s0 = 0; s0 < NS; s0++)
             for (int w2 = 0; w2 < kWarps; w2++) agg[s0] += S.warp_agg[w2][s0];
-        tst->func = S.tile_f;
+        tst->func = SPEC ? (S.tile_f | (kAllStates << 8)) : S.tile_f;
 #pragma unroll
         for (int s0 = 0; s0 < NS; s0++) tst->agg[s0] = agg[s0];
         st_release(&tst->flag, p.epoch * 4 + 1);
         for (int s0 = 0; s0 < 4; s0++) S.agg[s0] = agg[s0];
+        S.spec_p = kAllStates;
     }
 }
 
 // Block-wide look-back (all threads): thread t watches predecessor
 // tile - 1 - t. Waits only for the predecessors nearer than the nearest
-// published inclusive prefix.
-template <int NS>
-__device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t &entry, uint32_t pre[3]) {
+// published inclusive prefix (level kIncl); returns the tile's entry state,
+// the counts of the file before it and, for speculative aggregates, whether
+// some of those counts are not known yet.
+//
+// Speculative status levels: 1 = the tile's full transfer function, the
+// entry state it assumed and its counts under that assumption; 2 = its true
+// exit state and its counts under its true entry (published by a tile whose
+// assumption was wrong, as soon as its look-back knows its entry); 3 = its
+// inclusive prefix. The entry state never waits on counts: it follows from
+// the transfer functions alone. A level-1 tile that assumed the wrong entry
+// makes the counts unknown until it reaches level 2.
+template <int NS, bool SPEC>
+__device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t &entry, uint32_t pre[3],
+                             bool &unknown) {
+    constexpr uint32_t kIncl = SPEC ? 3 : 2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     uint32_t af = kIdentity;  // thread 0: aggregate between the window and `tile`
-    uint64_t ac[4] = {0, 0, 0, 0};
+    uint32_t ac[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    uint32_t au = 0;
     const uint64_t t0 = globaltimer_ns();
+    unknown = false;
     if (tile == 0) {
         entry = 0;
         pre[0] = pre[1] = pre[2] = 0;
@@ -690,7 +809,7 @@ __device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t
             if (in) flag = ld_acquire(&p.status[j].flag);
             const bool cur = (flag >> 2) == p.epoch;
             const bool waitv = in && !(cur && (flag & 3) >= 1);
-            const bool incl = in && cur && (flag & 3) >= 2;
+            const bool incl = in && cur && (flag & 3) >= kIncl;
             const uint32_t bw = __ballot_sync(0xffffffffu, waitv), bi = __ballot_sync(0xffffffffu, incl);
             if (lane == 0 && bw) atomicMin(&S.lb_first_wait[sl], (uint32_t)(warp * 32 + __ffs(bw) - 1));
             if (lane == 0 && bi) atomicMin(&S.lb_first_incl[sl], (uint32_t)(warp * 32 + __ffs(bi) - 1));
@@ -712,9 +831,27 @@ __device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t
         uint32_t f = kIdentity;
         uint64_t c[4] = {0, 0, 0, 0};
         if (in && (uint32_t)tid < sidx) {
-            f = ld_relaxed(&p.status[j].func);
+            if (!SPEC) {
+                f = ld_relaxed(&p.status[j].func);
 #pragma unroll
-            for (int s0 = 0; s0 < NS; s0++) c[s0] = ld_relaxed64(&p.status[j].agg[s0]);
+                for (int s0 = 0; s0 < NS; s0++) c[s0] = ld_relaxed64(&p.status[j].agg[s0]);
+            } else if ((flag & 3) >= 2) {
+                f = fconst(ld_relaxed(&p.status[j].exit));
+                const uint64_t v = ld_relaxed64(&p.status[j].agg[1]);
+#pragma unroll
+                for (int s0 = 0; s0 < NS; s0++) c[s0] = v;
+            } else {
+                const uint32_t pf = ld_relaxed(&p.status[j].func);
+                f = pf & 0xFF;
+                if ((pf >> 8) == kAllStates) {
+#pragma unroll
+                    for (int s0 = 0; s0 < NS; s0++) c[s0] = ld_relaxed64(&p.status[j].agg[s0]);
+                } else {
+                    const uint64_t v = ld_relaxed64(&p.status[j].agg[0]);
+#pragma unroll
+                    for (int s0 = 0; s0 < NS; s0++) c[s0] = (uint32_t)s0 == (pf >> 8) ? v : kUnknown;
+                }
+            }
         }
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -722,7 +859,10 @@ __device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t
             uint64_t gc[4];
 #pragma unroll
             for (int s0 = 0; s0 < NS; s0++) gc[s0] = __shfl_down_sync(0xffffffffu, c[s0], d);
-            if (lane + d < 32) agg_prepend<NS>(gf, gc, f, c);
+            if (lane + d < 32) {
+                if (SPEC) agg_prepend_spec<NS>(gf, gc, f, c);
+                else agg_prepend<NS>(gf, gc, f, c);
+            }
         }
         if (lane == 0) {
             S.lb_wf[warp] = f;
@@ -737,32 +877,26 @@ __device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t
         }
         __syncthreads();
         if (tid == 0) {
-            uint32_t wf = kIdentity;
-            uint64_t wc[4] = {0, 0, 0, 0};
             for (int w = 0; w < kWarps; w++) {
-                uint64_t g[4];
+                unsigned long long g[4];
 #pragma unroll
                 for (int s0 = 0; s0 < NS; s0++) g[s0] = S.lb_wc[w][s0];
-                agg_prepend<NS>(S.lb_wf[w], g, wf, wc);
+                wide_prepend<NS>(S.lb_wf[w], g, af, ac, au);
             }
-            agg_prepend<NS>(wf, wc, af, ac);
             const bool found = sidx < (uint32_t)kThreads;
             const bool at_start = hi - kThreads < 0;
             S.lb_stop = found || at_start;
-            if (found) {
-                const uint32_t ex = S.lb_entry;
-                uint64_t cc = ac[0];
+            if (found || at_start) {
+                const uint32_t ex = found ? S.lb_entry : 0u;
+                uint32_t c0 = ac[0][0], c1 = ac[0][1], c2 = ac[0][2];
 #pragma unroll
-                for (int t = 1; t < NS; t++) cc = ex == (uint32_t)t ? ac[t] : cc;
-                S.lb_pre[0] += cfield(cc, 0);
-                S.lb_pre[1] += cfield(cc, 1);
-                S.lb_pre[2] += cfield(cc, 2);
+                for (int t = 1; t < NS; t++)
+                    if (ex == (uint32_t)t) { c0 = ac[t][0]; c1 = ac[t][1]; c2 = ac[t][2]; }
+                S.lb_pre[0] = (found ? S.lb_pre[0] : 0u) + c0;
+                S.lb_pre[1] = (found ? S.lb_pre[1] : 0u) + c1;
+                S.lb_pre[2] = (found ? S.lb_pre[2] : 0u) + c2;
                 S.lb_entry = fapply(af, ex);
-            } else if (at_start) {
-                S.lb_pre[0] = cfield(ac[0], 0);
-                S.lb_pre[1] = cfield(ac[0], 1);
-                S.lb_pre[2] = cfield(ac[0], 2);
-                S.lb_entry = fapply(af, 0);
+                S.lb_restart = (au >> ex) & 1u;
             }
         }
         __syncthreads();
@@ -772,26 +906,37 @@ __device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t
     pre[0] = S.lb_pre[0];
     pre[1] = S.lb_pre[1];
     pre[2] = S.lb_pre[2];
+    unknown = SPEC && S.lb_restart;
 }
 
 // Deferred output of one tile: inclusive prefix, staged index, tape.
-template <int D>
+// SPEC: a tile whose true entry (from the look-back) equals the one it
+// assumed reuses its local-pass masks; otherwise it re-derives them from
+// the true entry (the classified bytes are still in registers), publishes
+// its true exit and counts at once (level 2), and then its inclusive prefix
+// when every count before it is known.
+template <int D, bool SPEC>
 __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t tile, const LocalState &L) {
     constexpr int NS = NStates<D>::value;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t vs = (int64_t)tile * kTile - (int64_t)p.shift;
     uint32_t entry, pre[3];
-    lookback_cta<NS>(p, S, tile, entry, pre);
-    if (tid == 0) {
+    bool unknown;
+    lookback_cta<NS, SPEC>(p, S, tile, entry, pre, unknown);
+    const bool full = !SPEC || S.pspec_p == kAllStates;  // counted under every entry
+    const bool hit = full || entry == S.pspec_p;         // block-uniform
+    if (tid == 0 && hit && !unknown) {
         TileStatus *tst = &p.status[tile];
         unsigned long long mine = S.pagg[0];
+        if (full) {
 #pragma unroll
-        for (int t = 1; t < NS; t++) mine = entry == (uint32_t)t ? S.pagg[t] : mine;
+            for (int t = 1; t < NS; t++) mine = entry == (uint32_t)t ? S.pagg[t] : mine;
+        }
         tst->exit = fapply(S.ptile_f, entry);
         tst->incl[0] = pre[0] + cfield(mine, 0);
         tst->incl[1] = pre[1] + cfield(mine, 1);
         tst->incl[2] = pre[2] + cfield(mine, 2);
-        st_release(&tst->flag, p.epoch * 4 + 2);
+        st_release(&tst->flag, p.epoch * 4 + (SPEC ? 3 : 2));
         S.tile_c = mine;
         if (tile == p.num_tiles - 1) {
             p.hdr->n_struct = pre[0] + cfield(mine, 0);
@@ -800,11 +945,23 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
         }
     }
     const uint32_t s_in = fapply(L.excl, entry);
-    const uint64_t stm = structural_mask<D>(L.m, L.ls, s_in);
-    const uint64_t term = stm & L.m.nl;
-    unsigned long long c = L.cv[0];
+    if (p.states64) p.states64[(uint64_t)tile * kThreads + tid] = (uint8_t)s_in;
+    uint64_t stm;
+    unsigned long long c;
+    if (!full && hit) {
+        stm = L.stm;
+        c = L.cv[0];
+    } else {
+        stm = structural_mask<D>(L.m, L.ls, s_in);
+        if (!full) {
+            c = (unsigned long long)__popcll(stm) | ((unsigned long long)__popcll(stm & L.m.nl) << 21);
+        } else {
+            c = L.cv[0];
 #pragma unroll
-    for (int t = 1; t < NS; t++) c = s_in == (uint32_t)t ? L.cv[t] : c;
+            for (int t = 1; t < NS; t++) c = s_in == (uint32_t)t ? L.cv[t] : c;
+        }
+    }
+    const uint64_t term = stm & L.m.nl;
     const unsigned long long ci = warp_scan_sum(c, lane);
     if (lane == 31) S.warp_c[warp] = ci;
     unsigned long long ce = ci - c;
@@ -813,8 +970,45 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
         const unsigned long long wc = lane < kWarps ? S.warp_c[lane] : 0ull;
         const unsigned long long wi = warp_scan_sum(wc, lane);
         if (lane < kWarps) S.warp_c[lane] = wi - wc;
+        if (SPEC && !hit && lane == kWarps - 1) {
+            // wrong assumption: true exit and recount for the successors
+            TileStatus *tst = &p.status[tile];
+            tst->exit = fapply(S.ptile_f, entry);
+            tst->agg[1] = wi;
+            st_release(&tst->flag, p.epoch * 4 + 2);
+            atomicAdd(&p.hdr->spec_repairs, 1ull);
+        }
+        if (SPEC && lane == kWarps - 1) S.tile_c = wi;
     }
     __syncthreads();
+    if (SPEC && (!hit || unknown)) {
+        // wait until every count before the tile is known, then publish
+        const uint64_t t0 = globaltimer_ns();
+        while (unknown) {
+            if (__syncthreads_or(tid == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs))) {
+                if (tid == 0) fail(p.hdr, ERR_TIMEOUT);
+                break;
+            }
+            __nanosleep(128);
+            uint32_t e2;
+            lookback_cta<NS, SPEC>(p, S, tile, e2, pre, unknown);
+        }
+        if (tid == 0) {
+            const unsigned long long mine = S.tile_c;
+            TileStatus *tst = &p.status[tile];
+            if (hit) tst->exit = fapply(S.ptile_f, entry);
+            tst->incl[0] = pre[0] + cfield(mine, 0);
+            tst->incl[1] = pre[1] + cfield(mine, 1);
+            tst->incl[2] = pre[2] + cfield(mine, 2);
+            st_release(&tst->flag, p.epoch * 4 + 3);
+            if (tile == p.num_tiles - 1) {
+                p.hdr->n_struct = pre[0] + cfield(mine, 0);
+                p.hdr->n_terms = pre[1] + cfield(mine, 1);
+                p.hdr->n_rows = pre[2] + cfield(mine, 2);
+            }
+        }
+        __syncthreads();
+    }
     ce += S.warp_c[warp];
     {
         uint32_t k = cfield(ce, 0);
@@ -854,7 +1048,7 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
     }
 }
 
-template <int D>
+template <int D, bool SPEC = false>
 __global__ void __launch_bounds__(kThreads) index_kernel(const Params p) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     SmemIx &S = *reinterpret_cast<SmemIx *>(smem_raw);
@@ -889,19 +1083,20 @@ __global__ void __launch_bounds__(kThreads) index_kernel(const Params p) {
                 break;
             }
             phase[s] ^= 1;
-            local_pass<D>(p, S, tile, S.buf[s], cur);
+            local_pass<D, SPEC>(p, S, tile, S.buf[s], cur);
             __syncthreads();  // buf[s] fully read
             if (tid == 0 && tile + 2 * G < p.num_tiles) {
                 fence_proxy_async();
                 issue_tile_ix(p, tile + 2 * G, S.buf[s], &S.bar[s]);
             }
         }
-        if (have_prev) output_pass<D>(p, S, prev_tile, prev);
+        if (have_prev) output_pass<D, SPEC>(p, S, prev_tile, prev);
         if (!has_cur) break;
         __syncthreads();
         if (tid == 0) {
             S.ptile_f = S.tile_f;
             for (int k = 0; k < 4; k++) S.pagg[k] = S.agg[k];
+            S.pspec_p = S.spec_p;
         }
         __syncthreads();
         prev = cur;
@@ -970,6 +1165,7 @@ struct falx_ctx {
     cudaStream_t stream = nullptr;
     int sm_count = 0;
     int blocks_per_sm[5][2] = {};
+    int blocks_per_sm_spec[5] = {};
     int ctas_per_sm = 0;  // FALX_CTAS_PER_SM caps the persistent grid (tuning)
     TileStatus *status = nullptr;
     ArenaStatus *astatus = nullptr;
@@ -984,6 +1180,11 @@ struct falx_ctx {
     uint64_t dev_out_cap = 0;
     NdjsonAcc *nd_acc = nullptr;   // device
     NdjsonAcc *nd_host = nullptr;  // pinned
+    // entry-region predictor: activations and classes for `mlp_cap` samples
+    uint8_t *mlp_scratch = nullptr;
+    uint64_t mlp_cap = 0;
+    uint8_t *pred = nullptr;  // predicted entry state per tile
+    uint64_t pred_cap = 0;
 };
 
 namespace {
@@ -998,6 +1199,16 @@ int cuda_fail(cudaError_t e) {
         cudaError_t e_ = (x);                \
         if (e_ != cudaSuccess) return cuda_fail(e_); \
     } while (0)
+
+template <int D>
+int setup_spec_kernel(falx_ctx *c) {
+    const void *fn = (const void *)index_kernel<D, true>;
+    FALX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemIx)));
+    int nb = 0;
+    FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, sizeof(SmemIx)));
+    c->blocks_per_sm_spec[D] = nb > 0 ? nb : 1;
+    return FALX_OK;
+}
 
 template <int D, bool ROWS>
 int setup_kernel(falx_ctx *c) {
@@ -1034,7 +1245,7 @@ int ensure_status(falx_ctx *c, uint32_t tiles) {
 bool valid_dialect(int d) { return d >= FALX_CSV && d <= FALX_NDJSON; }
 
 // Launch the scan over [data, data+len) with the outputs in `P` (device).
-int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t len, Params P) {
+int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t len, Params P, bool spec = false) {
     uint64_t shift = (uint64_t)((uintptr_t)data & 15u);
     uint64_t tiles64 = (len + shift + kTile - 1) / kTile;
     uint32_t tiles = (uint32_t)tiles64;
@@ -1051,7 +1262,7 @@ int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t 
     P.astatus = c->astatus;
     P.hdr = c->hdr;
     P.halo = rows ? kHaloBytes : 0;
-    int nb = c->blocks_per_sm[dialect][rows ? 1 : 0];
+    int nb = spec ? c->blocks_per_sm_spec[dialect] : c->blocks_per_sm[dialect][rows ? 1 : 0];
     if (c->ctas_per_sm > 0 && c->ctas_per_sm < nb) nb = c->ctas_per_sm;
     uint64_t grid = (uint64_t)c->sm_count * (uint64_t)nb;
     if (grid > tiles) grid = tiles;
@@ -1062,6 +1273,9 @@ int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t 
         if (rows)                                                                                 \
             err = cudaLaunchCooperativeKernel((const void *)scan_kernel<D, true>, dim3((unsigned)grid), \
                                               dim3(kThreads), args_, sizeof(Smem<true>), c->stream);     \
+        else if (spec)                                                                            \
+            err = cudaLaunchCooperativeKernel((const void *)index_kernel<D, true>, dim3((unsigned)grid), \
+                                              dim3(kThreads), args_, sizeof(SmemIx), c->stream);         \
         else                                                                                      \
             err = cudaLaunchCooperativeKernel((const void *)index_kernel<D>, dim3((unsigned)grid),     \
                                               dim3(kThreads), args_, sizeof(SmemIx), c->stream);         \
@@ -1243,7 +1457,8 @@ int falx_create(int device, falx_ctx **out) {
     if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) rc = FALX_ERR_CUDA;
 #define FALX_SETUP(D)                                  \
     if (!rc) rc = setup_kernel<D, false>(c);           \
-    if (!rc) rc = setup_kernel<D, true>(c);
+    if (!rc) rc = setup_kernel<D, true>(c);            \
+    if (!rc) rc = setup_spec_kernel<D>(c);
     FALX_SETUP(D_CSV) FALX_SETUP(D_CSV_HASH) FALX_SETUP(D_TSV) FALX_SETUP(D_LOGFMT) FALX_SETUP(D_NDJSON)
 #undef FALX_SETUP
     if (!rc && cudaMalloc(&c->hdr, sizeof(DevHeader)) != cudaSuccess) rc = FALX_ERR_CUDA;
@@ -1271,6 +1486,8 @@ void falx_destroy(falx_ctx *c) {
     if (c->dev_out) cudaFree(c->dev_out);
     if (c->nd_acc) cudaFree(c->nd_acc);
     if (c->nd_host) cudaFreeHost(c->nd_host);
+    if (c->mlp_scratch) cudaFree(c->mlp_scratch);
+    if (c->pred) cudaFree(c->pred);
     delete c;
 }
 
@@ -1476,6 +1693,396 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     host_out->n_seps = d.n_seps;
     host_out->n_ends = d.n_ends;
     return r2 ? r2 : rc;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Learned speculation: the entry-region predictor and the speculative index.
+// ===========================================================================
+struct falx_model {
+    int device = 0;
+    falx::mlp::Model m;
+    float *grad = nullptr;  // gradient scratch [kParams]
+    float *loss = nullptr;  // device scalar
+    float min_prob = 0.f;   // tile predictions less likely than this assume nothing
+};
+
+namespace {
+
+using namespace falx::mlp;
+
+// Scratch for n samples: classes, activations, gradients.
+struct MlpScratch {
+    uint8_t *cls, *label;
+    Acts a;
+};
+
+uint64_t mlp_bytes(uint64_t n) {
+    auto al = [](uint64_t b) { return (b + 255) & ~255ull; };
+    return al(n * kPos) + al(n) + 4 * al(n * kHid * 4) + 2 * al(n * kHid * 2) + 2 * al(n * kOut * 4) + al(4);
+}
+
+int mlp_scratch(falx_ctx *c, uint64_t n, MlpScratch &s) {
+    const uint64_t need = mlp_bytes(n);
+    if (need > c->mlp_cap) {
+        if (c->mlp_scratch) cudaFree(c->mlp_scratch);
+        c->mlp_scratch = nullptr;
+        c->mlp_cap = 0;
+        FALX_CUDA(cudaMalloc(&c->mlp_scratch, need));
+        c->mlp_cap = need;
+    }
+    uint8_t *p = c->mlp_scratch;
+    auto take = [&](uint64_t b) {
+        uint8_t *r = p;
+        p += (b + 255) & ~255ull;
+        return r;
+    };
+    s.cls = take(n * kPos);
+    s.label = take(n);
+    s.a.a1 = (float *)take(n * kHid * 4);
+    s.a.a2 = (float *)take(n * kHid * 4);
+    s.a.d2 = (float *)take(n * kHid * 4);
+    s.a.d1 = (float *)take(n * kHid * 4);
+    s.a.h1 = (__nv_bfloat16 *)take(n * kHid * 2);
+    s.a.h2 = (__nv_bfloat16 *)take(n * kHid * 2);
+    s.a.z = (float *)take(n * kOut * 4);
+    s.a.dz = (float *)take(n * kOut * 4);
+    s.a.loss = (float *)take(4);
+    return FALX_OK;
+}
+
+unsigned blocks(uint64_t n, unsigned per) { return (unsigned)((n + per - 1) / per); }
+
+int refresh(falx_ctx *c, falx_model *md) {
+    refresh_bf16<<<blocks((uint64_t)kIn * kHid, 256), 256, 0, c->stream>>>(md->m.w, md->m.w1, md->m.w1t, md->m.w2,
+                                                                          md->m.w2t, md->m.w3);
+    return cuda_fail(cudaGetLastError());
+}
+
+// Forward pass of n samples whose classes are in `cls`; keeps the
+// pre-activations when `train`.
+int mlp_forward(falx_ctx *c, const falx_model *md, const uint8_t *cls, uint32_t n, Acts &a, bool train, uint8_t *pred) {
+    if (n == 0) return FALX_OK;
+    l1_forward<<<blocks(n, kL1Samples), kHid, 0, c->stream>>>(cls, n, md->m.w1, md->m.w + kOffB1,
+                                                              train ? a.a1 : nullptr, a.h1);
+    l2_forward<<<blocks(n, kL2Samples), kHid, 0, c->stream>>>(a.h1, n, md->m.w2, md->m.w + kOffB2,
+                                                              train ? a.a2 : nullptr, a.h2);
+    l3_forward<<<blocks((uint64_t)n * 32, 256), 256, 0, c->stream>>>(a.h2, n, md->m.w3, md->m.w + kOffB3, a.z, pred);
+    return cuda_fail(cudaGetLastError());
+}
+
+// Inference on the tensor cores: samples are the 256 bytes at
+// first + s * stride of `data`, or the classes in `cls`.
+int mlp_infer(falx_ctx *c, const falx_model *md, const uint8_t *data, uint64_t len, int64_t first, int64_t stride,
+              const uint8_t *cls, uint32_t n, Acts &a, float *z, uint8_t *pred, float min_prob) {
+    if (n == 0) return FALX_OK;
+    const unsigned grid = blocks(n, kMmaRows);
+    mma_layer<true><<<grid, kMmaThreads, sizeof(MmaSmem), c->stream>>>(data, len, first, stride, cls, nullptr, n,
+                                                                        md->m.w1t, md->m.w + kOffB1, a.h1);
+    mma_layer<false><<<grid, kMmaThreads, sizeof(MmaSmem), c->stream>>>(nullptr, 0, 0, 0, nullptr, a.h1, n, md->m.w2t,
+                                                                         md->m.w + kOffB2, a.h2);
+    l3_forward<<<blocks((uint64_t)n * 32, 256), 256, 0, c->stream>>>(a.h2, n, md->m.w3, md->m.w + kOffB3, z, pred,
+                                                                      min_prob);
+    return cuda_fail(cudaGetLastError());
+}
+
+// Gradient of the mean cross-entropy of n labelled samples into g.
+int mlp_grad(falx_ctx *c, const falx_model *md, const uint8_t *cls, const uint8_t *label, uint32_t n, Acts &a,
+             float *g) {
+    int rc = mlp_forward(c, md, cls, n, a, true, nullptr);
+    if (rc) return rc;
+    FALX_CUDA(cudaMemsetAsync(a.loss, 0, 4, c->stream));
+    xent_kernel<<<blocks(n, 256), 256, 0, c->stream>>>(a.z, label, n, a.dz, a.loss);
+    const unsigned g3 = n < 1024 ? n : 1024;
+    l3_backward<<<g3, kHid, 0, c->stream>>>(a.h2, a.a2, a.dz, n, md->m.w3, g, a.d2);
+    l2_wgrad<<<kHid, kHid, 0, c->stream>>>(a.h1, a.d2, n, g);
+    l2_dgrad<<<blocks(n, kL2Samples), kHid, 0, c->stream>>>(a.d2, a.a1, n, md->m.w2t, a.d1);
+    l1_wgrad<<<kPos, kHid, 0, c->stream>>>(cls, a.d1, n, g);
+    return cuda_fail(cudaGetLastError());
+}
+
+// splitmix64 for the initial weights.
+uint64_t mix64(uint64_t &x) {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+int tile_count(const uint8_t *data, uint64_t len, uint32_t &tiles, uint64_t &shift) {
+    shift = (uint64_t)((uintptr_t)data & 15u);
+    tiles = (uint32_t)((len + shift + kTile - 1) / kTile);
+    return FALX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint64_t falx_model_param_count(void) { return kParams; }
+
+int falx_model_create(falx_ctx *c, uint64_t seed, falx_model **out) {
+    if (!c || !out) return FALX_ERR_INVALID;
+    *out = nullptr;
+    FALX_CUDA(cudaSetDevice(c->device));
+    falx_model *md = new (std::nothrow) falx_model;
+    if (!md) return FALX_ERR_INVALID;
+    md->device = c->device;
+    float *host = (float *)calloc(kParams, sizeof(float));
+    int rc = host ? FALX_OK : FALX_ERR_INVALID;
+    if (!rc) {
+        // uniform(-r, r) with r = sqrt(6 / active inputs); biases zero
+        uint64_t x = seed;
+        auto fill = [&](uint64_t off, uint64_t count, float r) {
+            for (uint64_t i = 0; i < count; i++) {
+                const double u = (double)(mix64(x) >> 11) * (1.0 / 9007199254740992.0);
+                host[off + i] = (float)((2.0 * u - 1.0) * r);
+            }
+        };
+        fill(kOffW1, (uint64_t)kIn * kHid, sqrtf(6.f / kPos));
+        fill(kOffW2, (uint64_t)kHid * kHid, sqrtf(6.f / kHid));
+        fill(kOffW3, (uint64_t)kHid * kOut, sqrtf(6.f / (kHid + kOut)));
+    }
+    auto alloc = [&](void **p, uint64_t b) {
+        if (!rc && cudaMalloc(p, b) != cudaSuccess) rc = FALX_ERR_CUDA;
+    };
+    alloc((void **)&md->m.w, kParams * 4);
+    alloc((void **)&md->m.m, kParams * 4);
+    alloc((void **)&md->m.v, kParams * 4);
+    alloc((void **)&md->grad, kParams * 4);
+    alloc((void **)&md->loss, 4);
+    alloc((void **)&md->m.w1, (uint64_t)kIn * kHid * 2);
+    alloc((void **)&md->m.w1t, (uint64_t)kIn * kHid * 2);
+    if (!rc && (cudaFuncSetAttribute((const void *)mma_layer<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(MmaSmem)) != cudaSuccess ||
+                cudaFuncSetAttribute((const void *)mma_layer<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(MmaSmem)) != cudaSuccess))
+        rc = FALX_ERR_CUDA;
+    alloc((void **)&md->m.w2, (uint64_t)kHid * kHid * 2);
+    alloc((void **)&md->m.w2t, (uint64_t)kHid * kHid * 2);
+    alloc((void **)&md->m.w3, (uint64_t)kHid * kOut * 2);
+    if (!rc && cudaMemcpyAsync(md->m.w, host, kParams * 4, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+        rc = FALX_ERR_CUDA;
+    if (!rc && cudaMemsetAsync(md->m.m, 0, kParams * 4, c->stream) != cudaSuccess) rc = FALX_ERR_CUDA;
+    if (!rc && cudaMemsetAsync(md->m.v, 0, kParams * 4, c->stream) != cudaSuccess) rc = FALX_ERR_CUDA;
+    if (!rc) rc = refresh(c, md);
+    if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = FALX_ERR_CUDA;
+    free(host);
+    if (rc) {
+        falx_model_destroy(md);
+        (void)cudaGetLastError();
+        return rc;
+    }
+    *out = md;
+    return FALX_OK;
+}
+
+void falx_model_destroy(falx_model *md) {
+    if (!md) return;
+    cudaSetDevice(md->device);
+    void *ps[] = {md->m.w, md->m.m, md->m.v, md->grad, md->loss, md->m.w1, md->m.w1t, md->m.w2, md->m.w2t, md->m.w3};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    delete md;
+}
+
+int falx_model_set_confidence(falx_model *md, float min_prob) {
+    if (!md || !(min_prob >= 0.f && min_prob <= 1.f)) return FALX_ERR_INVALID;
+    md->min_prob = min_prob;
+    return FALX_OK;
+}
+
+int falx_model_get(falx_ctx *c, const falx_model *md, float *host, uint64_t n) {
+    if (!c || !md || !host || n != kParams) return FALX_ERR_INVALID;
+    FALX_CUDA(cudaMemcpyAsync(host, md->m.w, kParams * 4, cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    return FALX_OK;
+}
+
+int falx_model_set(falx_ctx *c, falx_model *md, const float *host, uint64_t n) {
+    if (!c || !md || !host || n != kParams) return FALX_ERR_INVALID;
+    FALX_CUDA(cudaMemcpyAsync(md->m.w, host, kParams * 4, cudaMemcpyHostToDevice, c->stream));
+    FALX_CUDA(cudaMemsetAsync(md->m.m, 0, kParams * 4, c->stream));
+    FALX_CUDA(cudaMemsetAsync(md->m.v, 0, kParams * 4, c->stream));
+    md->m.step = 0;
+    int rc = refresh(c, md);
+    if (rc) return rc;
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    return FALX_OK;
+}
+
+int falx_byte_classes(falx_ctx *c, const uint8_t *data, uint64_t len, const int64_t *starts, uint32_t n,
+                      uint8_t *cls) {
+    if (!c || (len && !data) || (n && (!starts || !cls))) return FALX_ERR_INVALID;
+    if (n == 0) return FALX_OK;
+    classes_kernel<<<blocks((uint64_t)n * kPos, 256), 256, 0, c->stream>>>(data, len, starts, 0, 0, n, cls);
+    FALX_CUDA(cudaGetLastError());
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    return FALX_OK;
+}
+
+int falx_model_forward(falx_ctx *c, const falx_model *md, const uint8_t *cls, uint32_t n, float *logits,
+                       uint8_t *pred) {
+    if (!c || !md || (n && !cls) || ((uintptr_t)cls & 15)) return FALX_ERR_INVALID;
+    MlpScratch s;
+    int rc = mlp_scratch(c, n, s);
+    if (rc) return rc;
+    rc = mlp_infer(c, md, nullptr, 0, 0, 0, cls, n, s.a, s.a.z, pred, 0.f);
+    if (rc) return rc;
+    if (logits && n) FALX_CUDA(cudaMemcpyAsync(logits, s.a.z, (uint64_t)n * kOut * 4, cudaMemcpyDeviceToDevice,
+                                               c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    return FALX_OK;
+}
+
+int falx_model_grad(falx_ctx *c, const falx_model *md, const uint8_t *cls, const uint8_t *labels, uint32_t n,
+                    float *grad, float *loss) {
+    if (!c || !md || !cls || !labels || !grad || n == 0) return FALX_ERR_INVALID;
+    MlpScratch s;
+    int rc = mlp_scratch(c, n, s);
+    if (rc) return rc;
+    rc = mlp_grad(c, md, cls, labels, n, s.a, grad);
+    if (rc) return rc;
+    float l = 0;
+    FALX_CUDA(cudaMemcpyAsync(&l, s.a.loss, 4, cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    if (loss) *loss = l;
+    return FALX_OK;
+}
+
+int falx_model_train(falx_ctx *c, falx_model *md, const uint8_t *cls, const uint8_t *labels, uint64_t n,
+                     uint32_t batch, uint32_t epochs, float lr, float *last_loss) {
+    if (!c || !md || !cls || !labels || n == 0 || batch == 0) return FALX_ERR_INVALID;
+    MlpScratch s;
+    int rc = mlp_scratch(c, batch, s);
+    if (rc) return rc;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    float l = 0;
+    for (uint32_t e = 0; e < epochs; e++) {
+        for (uint64_t at = 0; at + batch <= n; at += batch) {
+            rc = mlp_grad(c, md, cls + at * kPos, labels + at, batch, s.a, md->grad);
+            if (rc) return rc;
+            md->m.step++;
+            const float c1 = 1.f - powf(b1, (float)md->m.step), c2 = 1.f - powf(b2, (float)md->m.step);
+            adam_kernel<<<blocks(kParams, 256), 256, 0, c->stream>>>(md->m.w, md->m.m, md->m.v, md->grad, kParams,
+                                                                      lr, b1, b2, eps, c1, c2);
+            rc = refresh(c, md);
+            if (rc) return rc;
+        }
+    }
+    FALX_CUDA(cudaMemcpyAsync(&l, s.a.loss, 4, cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    if (last_loss) *last_loss = l;
+    return FALX_OK;
+}
+
+int falx_region_states(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, uint8_t *states, uint64_t cap,
+                       uint64_t *n_out) {
+    int rc = check_common(c, dialect, data, len);
+    if (rc) return rc;
+    if (!n_out) return FALX_ERR_INVALID;
+    uint32_t tiles;
+    uint64_t shift;
+    tile_count(data, len, tiles, shift);
+    *n_out = (uint64_t)tiles * kThreads;
+    if (len == 0) return FALX_OK;
+    if (cap < *n_out || !states) return FALX_ERR_CAPACITY;
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.states64 = states;
+    return run_scan(c, dialect, false, data, len, P);
+}
+
+int falx_predict_tiles(falx_ctx *c, const falx_model *md, const uint8_t *data, uint64_t len, uint8_t *pred,
+                       uint64_t cap, uint64_t *n_tiles) {
+    if (!c || !md || !n_tiles || (len && !data)) return FALX_ERR_INVALID;
+    uint32_t tiles;
+    uint64_t shift;
+    tile_count(data, len, tiles, shift);
+    *n_tiles = tiles;
+    if (tiles == 0) return FALX_OK;
+    if (cap < tiles || !pred) return FALX_ERR_CAPACITY;
+    MlpScratch s;
+    int rc = mlp_scratch(c, tiles, s);
+    if (rc) return rc;
+    rc = mlp_infer(c, md, data, len, -(int64_t)shift, kTile, nullptr, tiles, s.a, nullptr, pred, md->min_prob);
+    if (rc) return rc;
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    return FALX_OK;
+}
+
+int falx_index_structurals_assumed(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len,
+                                   const uint8_t *assumed, uint32_t *out, uint64_t cap, uint64_t *n_out,
+                                   falx_spec_stats *stats) {
+    int rc = check_common(c, dialect, data, len);
+    if (rc) return rc;
+    if (!n_out || (cap && !out)) return FALX_ERR_INVALID;
+    uint32_t tiles;
+    uint64_t shift;
+    tile_count(data, len, tiles, shift);
+    *n_out = 0;
+    if (stats) memset(stats, 0, sizeof *stats);
+    if (len == 0) return FALX_OK;
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.index = cap ? out : nullptr;
+    P.index_cap = cap;
+    P.pred = assumed;
+    rc = run_scan(c, dialect, false, data, len, P, true);
+    if (rc) return rc;
+    const DevHeader &h = *c->hhdr;
+    *n_out = h.n_struct;
+    if (stats) {
+        stats->tiles = tiles;
+        stats->mispredicted = h.spec_repairs;
+    }
+    if (h.n_struct > cap) return FALX_ERR_CAPACITY;
+    return FALX_OK;
+}
+
+int falx_index_structurals_speculative(falx_ctx *c, const falx_model *md, int dialect, const uint8_t *data,
+                                       uint64_t len, uint32_t *out, uint64_t cap, uint64_t *n_out,
+                                       falx_spec_stats *stats) {
+    int rc = check_common(c, dialect, data, len);
+    if (rc) return rc;
+    if (!n_out || (cap && !out)) return FALX_ERR_INVALID;
+    uint32_t tiles;
+    uint64_t shift;
+    tile_count(data, len, tiles, shift);
+    *n_out = 0;
+    if (stats) memset(stats, 0, sizeof *stats);
+    if (len == 0) return FALX_OK;
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.index = cap ? out : nullptr;
+    P.index_cap = cap;
+    if (md) {
+        if (tiles > c->pred_cap) {
+            if (c->pred) cudaFree(c->pred);
+            c->pred = nullptr;
+            c->pred_cap = 0;
+            FALX_CUDA(cudaMalloc(&c->pred, tiles));
+            c->pred_cap = tiles;
+        }
+        MlpScratch s;
+        rc = mlp_scratch(c, tiles, s);
+        if (rc) return rc;
+        rc = mlp_infer(c, md, data, len, -(int64_t)shift, kTile, nullptr, tiles, s.a, nullptr, c->pred,
+                       md->min_prob);
+        if (rc) return rc;
+        P.pred = c->pred;
+    }
+    rc = run_scan(c, dialect, false, data, len, P, true);
+    if (rc) return rc;
+    const DevHeader &h = *c->hhdr;
+    *n_out = h.n_struct;
+    if (stats) {
+        stats->tiles = tiles;
+        stats->mispredicted = h.spec_repairs;
+    }
+    if (h.n_struct > cap) return FALX_ERR_CAPACITY;
+    return FALX_OK;
 }
 
 }  // extern "C"

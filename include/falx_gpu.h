@@ -181,6 +181,79 @@ int falx_index_structurals_host(falx_ctx *ctx, int dialect, const uint8_t *host_
 int falx_parse_host(falx_ctx *ctx, const falx_schema *schema, const uint8_t *host_data, uint64_t len,
                     falx_outputs *host_out);
 
+/* ---------------------------------------------------------------------------
+ * Learned speculation. The reference's parallel drivers guess each chunk's
+ * entry state ("outside quotes") and re-index chunks whose guess was wrong
+ * (csv_geo.rs:95-149 speculative parity; csv_hash.rs:152-214 instead runs a
+ * full transfer-function prepass). Here a small MLP predicts every 16 KiB
+ * tile's entry region from its 256 leading bytes; the speculative index scans
+ * each tile under its predicted entry only, the exact look-back verifies every
+ * prediction, and a tile whose prediction was wrong re-derives its masks from
+ * the true entry before it publishes. Output is identical to
+ * falx_index_structurals whatever the predictions are.
+ *
+ * Model: 256 bytes -> one-hot over 8 byte classes ('"' '#' '\n' ',' '\r'
+ * digit letter other) -> 256 ReLU -> 256 ReLU -> 3 (NORMAL / QUOTE /
+ * COMMENT), BF16 operands, FP32 accumulation and softmax. Parameters are one
+ * FP32 vector: W1[2048][256] (row = byte * 8 + class), b1[256],
+ * W2[256][256] (in, out), b2[256], W3[256][3], b3[3].
+ * ------------------------------------------------------------------------- */
+#define FALX_MLP_BYTES 256
+#define FALX_SPEC_TILE 16384
+typedef struct falx_model falx_model;
+
+typedef struct {
+    uint64_t tiles;
+    uint64_t mispredicted; /* tiles re-derived from their true entry state */
+} falx_spec_stats;
+
+uint64_t falx_model_param_count(void);
+/* Random initial weights (uniform, scaled by fan-in) from `seed`. */
+int falx_model_create(falx_ctx *ctx, uint64_t seed, falx_model **out);
+void falx_model_destroy(falx_model *model);
+/* Tiles whose predicted state has softmax probability below `min_prob`
+ * assume nothing: they count under every entry state, like the plain scan,
+ * and can never be mispredicted (default 0: always take the arg-max). */
+int falx_model_set_confidence(falx_model *model, float min_prob);
+/* Copy the FP32 parameter vector out / in (host buffers of
+ * falx_model_param_count() floats). Setting resets the optimiser. */
+int falx_model_get(falx_ctx *ctx, const falx_model *model, float *host, uint64_t n);
+int falx_model_set(falx_ctx *ctx, falx_model *model, const float *host, uint64_t n);
+/* Byte classes of the FALX_MLP_BYTES bytes from each of n start offsets
+ * (device int64 array) into cls[n][256]; bytes outside the input are class 7. */
+int falx_byte_classes(falx_ctx *ctx, const uint8_t *data, uint64_t len, const int64_t *starts, uint32_t n,
+                      uint8_t *cls);
+/* Forward pass: logits[n][3] and/or the arg-max state (either may be NULL);
+ * `cls` 16-byte aligned. */
+int falx_model_forward(falx_ctx *ctx, const falx_model *model, const uint8_t *cls, uint32_t n, float *logits,
+                       uint8_t *pred);
+/* Gradient of the mean softmax cross-entropy over n labelled samples into
+ * grad[falx_model_param_count()] (device); *loss = the mean loss. */
+int falx_model_grad(falx_ctx *ctx, const falx_model *model, const uint8_t *cls, const uint8_t *labels, uint32_t n,
+                    float *grad, float *loss);
+/* Adam over `epochs` passes of n samples in minibatches of `batch`. */
+int falx_model_train(falx_ctx *ctx, falx_model *model, const uint8_t *cls, const uint8_t *labels, uint64_t n,
+                     uint32_t batch, uint32_t epochs, float lr, float *last_loss);
+/* Labels from the exact scan: the region state at the start of every
+ * 64-byte block, entry k for file position 64k - (data & 15). */
+int falx_region_states(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len, uint8_t *states,
+                       uint64_t cap, uint64_t *n_out);
+/* Predicted entry state of every tile (tile t starts at 16384t - (data & 15)). */
+int falx_predict_tiles(falx_ctx *ctx, const falx_model *model, const uint8_t *data, uint64_t len, uint8_t *pred,
+                       uint64_t cap, uint64_t *n_tiles);
+/* Speculative structural index under caller-supplied assumed entry states
+ * (device array, one per tile; 0xFF = no assumption, count every entry
+ * state; other values outside the dialect's states read as 0; tile 0 always
+ * assumes the initial state). */
+int falx_index_structurals_assumed(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len,
+                                   const uint8_t *assumed, uint32_t *out, uint64_t cap, uint64_t *n_out,
+                                   falx_spec_stats *stats);
+/* Speculative structural index; `model` NULL assumes every tile starts
+ * outside any region (the reference's guess). */
+int falx_index_structurals_speculative(falx_ctx *ctx, const falx_model *model, int dialect, const uint8_t *data,
+                                       uint64_t len, uint32_t *out, uint64_t cap, uint64_t *n_out,
+                                       falx_spec_stats *stats);
+
 /* Structural index without any allocation (no counterpart in the
  * reference, whose callers are Rust code that allocates freely). For callers
  * that may not allocate device memory: the look-back scratch is a fixed

@@ -295,3 +295,21 @@ def test_fused_parse_generated(engine, kind, dialect):
     compare_columns(got["columns"], rows, want, GEO_COLS)
     fb = got["field_bytes"]
     assert (fb.fields, fb.bytes) == oracle.field_bytes(doc, dialect)
+
+
+@pytest.mark.parametrize("doc_kind", ["commas", "short_rows"])
+def test_dense_inputs_long_lookback(engine, doc_kind):
+    # Every tile dense with structurals over tens of MiB: look-back spans of
+    # hundreds of tiles sum counts well beyond one tile's 16384.
+    doc = b"," * (48 << 20) + b"\n" if doc_kind == "commas" else b"1,2\n" * (24 << 20)
+    for dialect in (fx.CSV, fx.CSV_HASH):
+        assert np.array_equal(gpu_index(engine, doc, dialect), oracle.index_spec(doc, dialect))
+    seps, ends = engine.parse_tape(doc, fx.CSV_HASH)
+    ws, we = oracle.parse_tape(doc, fx.CSV_HASH)
+    assert np.array_equal(seps.cpu().numpy().view(np.uint32), ws)
+    assert np.array_equal(ends.cpu().numpy().view(np.uint64), we)
+    if doc_kind == "short_rows":
+        cols = [(0, fx.I64), (1, fx.U32)]
+        got = engine.parse_columns(doc, fx.Schema(fx.CSV_HASH, cols))
+        rows, want = oracle.parse_columns(doc, fx.CSV_HASH, cols)
+        compare_columns(got, rows, want, cols)
