@@ -288,6 +288,8 @@ def bench_gpu(args):
     d2h = 4 * n_struct + rows * (4 + 4 + 8 + 8) + 5 * words * 8 + 4 * (rows + 1) + str_len
     e2e = {"value": round(n / GIB / e2e_s, 4), "unit": "GiB/s", "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h}
 
+    spec = None if args.no_spec else bench_speculation(eng, args)
+
     if rank != 0:
         return
     cpu = None
@@ -312,12 +314,75 @@ def bench_gpu(args):
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
         "field_bytes": {"fields": fb.fields, "bytes": fb.bytes},
+        "learned_speculation": spec,
         "wall_s": round(wall, 3),
     }
     print(json.dumps(line))
     eng.close()
     if dist:
         dist.destroy_process_group()
+
+
+def bench_speculation(eng, args):
+    """Learned speculation on the adversarial csv_hash workload (1 GiB,
+    device-resident): the plain structural index against predict + the
+    speculative index with a model trained here on separately seeded
+    documents, the constant 'outside any region' guess beside them; outputs
+    are compared for identity."""
+    import ctypes
+
+    import torch
+
+    import falx_gb300 as fx
+    from falx_gb300 import _lib, gen, speculation
+
+    model, info = speculation.train_model(eng, train_bytes=512 << 20, epochs=3, stride=512)
+    calib = gen.generate(gen.ADVERSARIAL, 128 << 20, seed=speculation.EVAL_SEED)
+    conf = speculation.calibrate_confidence(eng, model, calib)
+    host = gen.generate(gen.ADVERSARIAL, args.size)
+    data = torch.from_numpy(host.copy()).cuda()
+    n = data.numel()
+    cap = n // 3
+    idx = torch.empty(cap, dtype=torch.int32, device="cuda")
+    idx2 = torch.empty(cap, dtype=torch.int32, device="cuda")
+    cnt, cnt2 = ctypes.c_uint64(), ctypes.c_uint64()
+    st = _lib.falx_spec_stats()
+    ptr = ctypes.c_void_p(data.data_ptr())
+
+    def plain():
+        _lib.check(eng.lib.falx_index_structurals(eng.ctx, fx.CSV_HASH, ptr, n, ctypes.c_void_p(idx.data_ptr()), cap,
+                                                  ctypes.byref(cnt)), "falx_index_structurals")
+
+    def spec(m):
+        _lib.check(eng.lib.falx_index_structurals_speculative(eng.ctx, m, fx.CSV_HASH, ptr, n,
+                                                              ctypes.c_void_p(idx2.data_ptr()), cap,
+                                                              ctypes.byref(cnt2), ctypes.byref(st)),
+                   "falx_index_structurals_speculative")
+
+    reps = max(3, min(args.steps, 10))
+    t_plain = speculation.time_index(eng, plain, reps)
+    t_const = speculation.time_index(eng, lambda: spec(None), reps)
+    wrong_const = st.mispredicted
+    t_spec = speculation.time_index(eng, lambda: spec(model.ptr), reps)
+    wrong, tiles = st.mispredicted, st.tiles
+    identical = cnt.value == cnt2.value and bool(torch.equal(idx[: cnt.value], idx2[: cnt2.value]))
+    pred = model.predict_tiles(data)
+    hedged = int((pred == 255).sum())
+    t_pred = speculation.time_index(eng, lambda: model.predict_tiles(data), reps)
+    gib = n / GIB
+    return {
+        "workload": "adversarial csv_hash 1 GiB device-resident (20% quoted cells up to 4 KiB with '#' and "
+                    "newlines, 5% comment lines with '\"'): structural index",
+        "plain": {"value": round(gib / (t_plain / 1e3), 3), "unit": "GiB/s", "ms": round(t_plain, 4)},
+        "speculative": {"value": round(gib / (t_spec / 1e3), 3), "unit": "GiB/s", "ms": round(t_spec, 4),
+                        "predict_ms": round(t_pred, 4)},
+        "speedup_vs_plain": round(t_plain / t_spec, 4),
+        "constant_guess": {"value": round(gib / (t_const / 1e3), 3), "unit": "GiB/s",
+                           "mispredicted_tiles": int(wrong_const)},
+        "tiles": int(tiles), "mispredicted_tiles": int(wrong), "misprediction_rate": round(wrong / max(tiles, 1), 6),
+        "rerun_fraction": round(wrong / max(tiles, 1), 6), "hedged_tiles": hedged, "confidence": conf,
+        "output_identical": identical, "training": info,
+    }
 
 
 def main():
@@ -329,6 +394,7 @@ def main():
     ap.add_argument("--size", type=int, default=1 << 30)
     ap.add_argument("--cpu-sample", type=int, default=64 << 20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-spec", action="store_true", help="skip the learned-speculation comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         bench_reference(args)

@@ -65,6 +65,17 @@ class falx_spec_stats(Structure):
     _fields_ = [("tiles", c_uint64), ("mispredicted", c_uint64)]
 
 
+class falx_doc(Structure):
+    _fields_ = [("data", c_void_p), ("len", c_uint64), ("dialect", c_int32), ("field0", c_uint32),
+                ("field1", c_uint32), ("index", c_void_p), ("index_cap", c_uint64), ("col0", c_void_p),
+                ("col1", c_void_p), ("valid0", c_void_p), ("valid1", c_void_p), ("rows_cap", c_uint64),
+                ("n_index", c_uint64), ("rows", c_uint64), ("status", c_int32)]
+
+
+class falx_batch_config(Structure):
+    _fields_ = [("chunk_bytes", c_uint32), ("ctas_per_sm", c_uint32), ("staging", c_uint32)]
+
+
 # Every symbol the header declares, with its signature.
 SIGNATURES = {
     "falx_create": (c_int, [c_int, POINTER(c_void_p)]),
@@ -102,6 +113,15 @@ SIGNATURES = {
                                                POINTER(c_uint64), POINTER(falx_spec_stats)]),
     "falx_index_structurals_speculative": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_uint64, c_void_p,
                                                    c_uint64, POINTER(c_uint64), POINTER(falx_spec_stats)]),
+    "falx_batch_create": (c_int, [c_void_p, POINTER(falx_doc), c_uint32, POINTER(falx_batch_config),
+                                  POINTER(c_void_p)]),
+    "falx_batch_run": (c_int, [c_void_p, POINTER(falx_doc)]),
+    "falx_batch_info": (c_int, [c_void_p, POINTER(falx_batch_config), POINTER(c_uint32), POINTER(c_uint32),
+                                POINTER(c_int)]),
+    "falx_batch_destroy": (None, [c_void_p]),
+    "falx_batch_tune": (c_int, [c_void_p, POINTER(falx_doc), c_uint32, POINTER(falx_batch_config),
+                                POINTER(c_float)]),
+    "falx_batch_plan": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, POINTER(c_uint32)]),
 }
 
 MLP_BYTES = 256

@@ -14,8 +14,9 @@ GPU_LIB = os.path.join(PKG, "libfalx_gpu.so")
 GEN_LIB = os.path.join(PKG, "libfalx_gen.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-GPU_SOURCES = ["falx_gpu.cu"]
-GPU_DEPS = ["scan_core.cuh", "rows.cuh", "decimal.cuh", "pow5_table.h", "ndjson.cuh", "mlp.cuh"]
+GPU_SOURCES = ["falx_gpu.cu", "batch.cu", "batch_nb2.cu", "batch_nb3.cu"]
+GPU_DEPS = ["scan_core.cuh", "rows.cuh", "decimal.cuh", "pow5_table.h", "ndjson.cuh", "mlp.cuh", "tile.cuh",
+            "context.h", "batch_kernel.cuh"]
 
 
 def _nvcc():
@@ -38,19 +39,29 @@ def _run(cmd):
 
 
 def build_gpu(force=False, verbose=False):
+    """Compile every translation unit (in parallel) and link the engine."""
     srcs = [os.path.join(CSRC, s) for s in GPU_SOURCES]
     deps = srcs + [os.path.join(CSRC, d) for d in GPU_DEPS] + [os.path.join(ROOT, "include", "falx_gpu.h")]
     if not force and not _stale(GPU_LIB, deps):
         return GPU_LIB
+    objdir = os.path.join(PKG, "_build")
+    os.makedirs(objdir, exist_ok=True)
+
+    def compile_one(src):
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
+        cmd = [_nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        r = _run(cmd)
+        if verbose:
+            print(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(len(srcs)) as ex:
+        objs = list(ex.map(compile_one, srcs))
     tmp = GPU_LIB + ".tmp"
-    cmd = [_nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
-                              "-o", tmp] + srcs
-    if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    r = _run(cmd)
+    _run([_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs)
     os.replace(tmp, GPU_LIB)
-    if verbose:
-        print(r.stderr)
     return GPU_LIB
 
 

@@ -1,0 +1,50 @@
+// Engine context (falx_ctx of the C ABI): device, stream, look-back
+// scratch and tuned launch parameters. Shared by the translation units of
+// the engine library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "tile.cuh"
+
+namespace falx {
+struct NdjsonAcc;
+}
+
+// Autotuned configuration of batched launches (falx_batch_tune).
+struct falx_batch_tuning {
+    int valid = 0;
+    uint32_t chunk_bytes = 0;  // documents up to this size run whole on one CTA
+    uint32_t ctas_per_sm = 0;
+    uint32_t staging = 0;      // tile buffers in flight per CTA
+};
+
+struct falx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    int blocks_per_sm[5][2] = {};
+    int blocks_per_sm_spec[5] = {};
+    int ctas_per_sm = 0;  // FALX_CTAS_PER_SM caps the persistent grid (tuning)
+    falx::TileStatus *status = nullptr;
+    falx::ArenaStatus *astatus = nullptr;
+    uint32_t status_cap = 0;
+    uint32_t epoch = 0;
+    falx::DevHeader *hdr = nullptr;   // device
+    falx::DevHeader *hhdr = nullptr;  // pinned host mirror
+    // staging for the host-buffer entry points
+    uint8_t *dev_in = nullptr;
+    uint64_t dev_in_cap = 0;
+    void *dev_out = nullptr;
+    uint64_t dev_out_cap = 0;
+    falx::NdjsonAcc *nd_acc = nullptr;   // device
+    falx::NdjsonAcc *nd_host = nullptr;  // pinned
+    // entry-region predictor: activations and classes for `mlp_cap` samples
+    uint8_t *mlp_scratch = nullptr;
+    uint64_t mlp_cap = 0;
+    uint8_t *pred = nullptr;  // predicted entry state per tile
+    uint64_t pred_cap = 0;
+    falx_batch_tuning batch_tuned;  // last autotuned batched-launch configuration
+};

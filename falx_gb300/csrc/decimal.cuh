@@ -24,7 +24,7 @@
 
 #ifdef __CUDACC__
 #define FALX_HD __host__ __device__ __forceinline__
-#define FALX_HD_NOINLINE __host__ __device__ __noinline__
+#define FALX_HD_NOINLINE static __host__ __device__ __noinline__
 #else
 #define FALX_HD static inline
 #define FALX_HD_NOINLINE static

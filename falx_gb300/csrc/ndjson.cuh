@@ -56,7 +56,7 @@ __device__ __forceinline__ bool j_string(const LineView &v, int64_t e, int64_t &
     return false;
 }
 
-__device__ bool j_skip_value(const LineView &v, int64_t e, int64_t &i) {
+__device__ inline bool j_skip_value(const LineView &v, int64_t e, int64_t &i) {
     j_ws(v, e, i);
     if (i >= e) return false;
     uint8_t c = v.at(i);
@@ -86,7 +86,7 @@ __device__ bool j_skip_value(const LineView &v, int64_t e, int64_t &i) {
 }
 
 // Position *i on the value of member `key` of the object opening at *i.
-__device__ bool j_member(const LineView &v, int64_t e, int64_t &i, const char *key, int klen) {
+__device__ inline bool j_member(const LineView &v, int64_t e, int64_t &i, const char *key, int klen) {
     if (i >= e || v.at(i) != '{') return false;
     i++;
     for (;;) {
@@ -109,7 +109,7 @@ __device__ bool j_member(const LineView &v, int64_t e, int64_t &i, const char *k
     }
 }
 
-__device__ bool j_int(const LineView &v, int64_t e, int64_t i, int64_t &out) {
+__device__ inline bool j_int(const LineView &v, int64_t e, int64_t i, int64_t &out) {
     bool neg = false;
     if (i < e && v.at(i) == '-') { neg = true; i++; }
     if (i >= e) return false;
@@ -127,7 +127,7 @@ __device__ bool j_int(const LineView &v, int64_t e, int64_t i, int64_t &out) {
     return true;
 }
 
-__device__ bool j_dec_e6(const LineView &v, int64_t e, int64_t i, int64_t &out) {
+__device__ inline bool j_dec_e6(const LineView &v, int64_t e, int64_t i, int64_t &out) {
     bool neg = false;
     if (i < e && v.at(i) == '-') { neg = true; i++; }
     uint64_t ip = 0;

@@ -264,7 +264,7 @@ __device__ __forceinline__ void stat_cell(StatAcc &a, int k, const uint8_t *s, u
 
 // String-arena look-back (one warp): returns, for each string column slot,
 // the arena bytes of the file before this tile; publishes the tile's totals.
-__device__ void arena_lookback(const RowCtx &rc, const uint32_t (&tot)[kMaxStr], int lane,
+__device__ inline void arena_lookback(const RowCtx &rc, const uint32_t (&tot)[kMaxStr], int lane,
                                unsigned long long (&pre)[kMaxStr]) {
     ArenaStatusView *as = static_cast<ArenaStatusView *>(rc.astatus);
     ArenaStatusView *me = &as[rc.tile];
@@ -332,7 +332,7 @@ __device__ void arena_lookback(const RowCtx &rc, const uint32_t (&tot)[kMaxStr],
 }
 
 // Block reduction of the sink accumulators into the call totals.
-__device__ void reduce_sinks(const RowSpec &rs, const RowCtx &rc, RowShared<true> &sh, const StatAcc &acc, int tid) {
+__device__ inline void reduce_sinks(const RowSpec &rs, const RowCtx &rc, RowShared<true> &sh, const StatAcc &acc, int tid) {
     const int lane = tid & 31, warp = tid >> 5;
     unsigned long long v[11] = {acc.fields, acc.bytes, acc.records, acc.values[0], acc.values[1],
                                 acc.checksum[0], acc.checksum[1], acc.sum_e6[0], acc.sum_e6[1],

@@ -73,3 +73,34 @@ def misprediction(engine, model, data, dialect=CSV_HASH):
     n = min(truth.numel(), pred.numel())
     truth, pred = truth[1:n], pred[1:n]  # tile 0's entry is known
     return {"tiles": n, "model_wrong": int((truth != pred).sum()), "constant_wrong": int((truth != 0).sum())}
+
+
+def time_index(engine, fn, reps=5):
+    """Best-of-reps device time (ms) of fn() on the current stream."""
+    torch = engine.torch
+    stream = torch.cuda.current_stream()
+    fn()
+    torch.cuda.synchronize()
+    best = float("inf")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(reps):
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return best
+
+
+def calibrate_confidence(engine, model, data, dialect=CSV_HASH, candidates=(0.0, 0.8, 0.9, 0.95, 0.98, 0.99)):
+    """Pick the hedging threshold with the fastest predict + speculative
+    scan on a calibration document (not the measured one)."""
+    d = engine.to_device(data)
+    best = None
+    for conf in candidates:
+        model.set_confidence(conf)
+        t = time_index(engine, lambda: engine.index_structurals_speculative(d, dialect, model=model), reps=3)
+        if best is None or t < best[1]:
+            best = (conf, t)
+    model.set_confidence(best[0])
+    return best[0]

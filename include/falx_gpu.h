@@ -254,6 +254,60 @@ int falx_index_structurals_speculative(falx_ctx *ctx, const falx_model *model, i
                                        uint64_t len, uint32_t *out, uint64_t cap, uint64_t *n_out,
                                        falx_spec_stats *stats);
 
+/* ---------------------------------------------------------------------------
+ * Batched documents: many documents of uneven sizes in one persistent launch
+ * from a device work queue, replayed from a CUDA graph. The reference parses
+ * one document per call (parse_columns_par / index_structurals_par per file,
+ * csv_geo.rs:1216-1284, :95-149); here a batch is planned once and each run
+ * gives every document the same outputs as falx_index_structurals plus two
+ * f64 columns (falx_parse_columns with two FALX_F64 columns).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    const uint8_t *data;  /* device, 16-byte aligned */
+    uint64_t len;
+    int32_t dialect;      /* FALX_CSV, FALX_TSV or FALX_LOGFMT */
+    uint32_t field0;      /* ordinals of the two f64 columns (e.g. lat, lon) */
+    uint32_t field1;
+    uint32_t *index;      /* structural index, index_cap entries (NULL / 0: none) */
+    uint64_t index_cap;
+    double *col0;         /* f64 columns and LSB-first validity, rows_cap rows (0: none) */
+    double *col1;
+    uint64_t *valid0;
+    uint64_t *valid1;
+    uint64_t rows_cap;
+    uint64_t n_index;     /* out */
+    uint64_t rows;        /* out */
+    int32_t status;       /* out: FALX_OK or an error of this document */
+} falx_doc;
+
+typedef struct {
+    uint32_t chunk_bytes; /* documents up to this size run whole on one CTA; larger ones tile by tile */
+    uint32_t ctas_per_sm; /* 0: as many as fit */
+    uint32_t staging;     /* tile buffers in flight per CTA: 2 or 3 */
+} falx_batch_config;
+
+typedef struct falx_batch falx_batch;
+
+/* Plan a batch on `docs` (device buffers stay the caller's; the batch
+ * records their addresses). cfg NULL: the context's last falx_batch_tune
+ * result, else defaults (1 MiB, all CTAs that fit, 2 buffers). */
+int falx_batch_create(falx_ctx *ctx, const falx_doc *docs, uint32_t ndocs, const falx_batch_config *cfg,
+                      falx_batch **out);
+/* One run of the planned batch (graph replay on the context's stream);
+ * fills n_index / rows / status of `docs` when not NULL. Returns the first
+ * document error, if any. */
+int falx_batch_run(falx_batch *batch, falx_doc *docs);
+int falx_batch_info(const falx_batch *batch, falx_batch_config *cfg, uint32_t *n_items, uint32_t *grid,
+                    int *graph);
+void falx_batch_destroy(falx_batch *batch);
+/* Time every candidate configuration (chunk 64 KiB..4 MiB, CTAs per SM,
+ * staging 2 / 3) on this batch; keep the fastest in the context. */
+int falx_batch_tune(falx_ctx *ctx, falx_doc *docs, uint32_t ndocs, falx_batch_config *best, float *best_ms);
+/* The work queue a batch would run (host only): items[3k..3k+2] =
+ * (document, first tile, end tile) for document lengths `lens`. */
+int falx_batch_plan(const uint64_t *lens, uint32_t ndocs, uint32_t chunk_bytes, uint32_t *items, uint32_t cap,
+                    uint32_t *n_items);
+
 /* Structural index without any allocation (no counterpart in the
  * reference, whose callers are Rust code that allocates freely). For callers
  * that may not allocate device memory: the look-back scratch is a fixed
