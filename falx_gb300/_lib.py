@@ -65,6 +65,11 @@ class falx_spec_stats(Structure):
     _fields_ = [("tiles", c_uint64), ("mispredicted", c_uint64)]
 
 
+class falx_shard_summary(Structure):
+    _fields_ = [("states", c_uint32), ("exit", c_uint32 * 4), ("structurals", c_uint64 * 4),
+                ("terminators", c_uint64 * 4), ("rows", c_uint64 * 4), ("last_byte", c_int32)]
+
+
 class falx_doc(Structure):
     _fields_ = [("data", c_void_p), ("len", c_uint64), ("dialect", c_int32), ("field0", c_uint32),
                 ("field1", c_uint32), ("index", c_void_p), ("index_cap", c_uint64), ("col0", c_void_p),
@@ -113,6 +118,10 @@ SIGNATURES = {
                                                POINTER(c_uint64), POINTER(falx_spec_stats)]),
     "falx_index_structurals_speculative": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_uint64, c_void_p,
                                                    c_uint64, POINTER(c_uint64), POINTER(falx_spec_stats)]),
+    "falx_summarize_shard": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_int, POINTER(falx_shard_summary)]),
+    "falx_parse_tape_seeded": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_int, c_uint32, c_uint64, c_uint64,
+                                       c_void_p, c_uint64, c_void_p, c_uint64, c_void_p, c_uint64,
+                                       POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64)]),
     "falx_batch_create": (c_int, [c_void_p, POINTER(falx_doc), c_uint32, POINTER(falx_batch_config),
                                   POINTER(c_void_p)]),
     "falx_batch_run": (c_int, [c_void_p, POINTER(falx_doc)]),

@@ -9,6 +9,7 @@ arenas; documents start 256-byte aligned in one device buffer.
 import ctypes
 import math
 import os
+from concurrent.futures import ThreadPoolExecutor
 from ctypes import byref, c_float, c_uint32, c_uint64, c_void_p
 
 import numpy as np
@@ -47,15 +48,18 @@ def generate(sizes, dialects, seed=0xD0C5, out=None):
         offs.append(pos)
         pos += (int(s) + ALIGN - 1) // ALIGN * ALIGN + ALIGN
     buf = out if out is not None else np.zeros(pos + (2 << 20), dtype=np.uint8)
-    lens = []
-    for k, (s, d) in enumerate(zip(sizes, dialects)):
-        cap = (int(s) + ALIGN - 1) // ALIGN * ALIGN + ALIGN
-        view = buf[offs[k]: offs[k] + cap]
-        doc = gen.generate(KIND_OF[int(d)], int(s), seed=seed + k, threads=1 if s < (8 << 20) else None,
-                           out=np.empty(int(s) + (1 << 20), dtype=np.uint8))
+
+    def one(k):
+        s, d = int(sizes[k]), int(dialects[k])
+        cap = (s + ALIGN - 1) // ALIGN * ALIGN + ALIGN
+        doc = gen.generate(KIND_OF[d], s, seed=seed + k, threads=1, out=np.empty(s + (1 << 20), dtype=np.uint8))
         n = min(doc.size, cap)
-        view[:n] = doc[:n]
-        lens.append(n)
+        buf[offs[k]: offs[k] + n] = doc[:n]
+        return n
+
+    # the generator releases the GIL: documents are written in parallel
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        lens = list(ex.map(one, range(len(sizes))))
     return buf, np.array(offs, dtype=np.int64), np.array(lens, dtype=np.int64)
 
 

@@ -47,4 +47,5 @@ struct falx_ctx {
     uint8_t *pred = nullptr;  // predicted entry state per tile
     uint64_t pred_cap = 0;
     falx_batch_tuning batch_tuned;  // last autotuned batched-launch configuration
+    void *summary_dev = nullptr;    // shard summary result (device)
 };

@@ -19,6 +19,7 @@
 //   ColumnSink / stats / field bytes      csv_geo.rs:952-1101, :1491-1770; csv_hash.rs:965-1435
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -81,7 +82,7 @@ struct SmemIx {
 // SPEC: the tile assumes the entry state p.pred[tile] (tile 0 assumes the
 // file's initial state), counts only under that assumption and publishes
 // its full transfer function, the assumed entry and those counts.
-template <int D, bool SPEC>
+template <int D, bool SPEC, bool CROWS = false>
 __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t tile, uint8_t *b, LocalState &L) {
     constexpr int kBuf = kPre + kTile;
     constexpr int NS = NStates<D>::value;
@@ -107,7 +108,7 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
     L.base_t = vs + (int64_t)tid * kThreadBytes;
     L.prev_nl = b[kPre + tid * kThreadBytes - 1] == '\n';
     L.ls = (L.m.nl << 1) | (uint64_t)L.prev_nl;
-    if (L.base_t <= 0 && L.base_t + kThreadBytes > 0) L.ls |= 1ull << (-L.base_t);
+    if (L.base_t <= 0 && L.base_t + kThreadBytes > 0 && starts_line(prev_of(p))) L.ls |= 1ull << (-L.base_t);
     const uint32_t f = thread_function<D>(L.m, L.ls);
     uint32_t incl = warp_scan_f(f, lane);
     if (lane == 31) S.warp_f[warp] = incl;
@@ -115,7 +116,7 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
     if (lane == 0) excl = kIdentity;
     if (!SPEC) {
 #pragma unroll
-        for (int e = 0; e < NS; e++) L.cv[e] = thread_counts<D, false>(L.m, L.ls, L.prev_nl, e, L.base_t, len);
+        for (int e = 0; e < NS; e++) L.cv[e] = thread_counts<D, CROWS>(L.m, L.ls, L.prev_nl, e, L.base_t, len, prev_of(p));
     }
     __syncthreads();
     if (warp == 0) {
@@ -130,13 +131,13 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
     L.excl = fcompose(S.warp_f[warp], excl);
     uint32_t pk = kAllStates;
     if (SPEC) {
-        pk = (tile == 0 || !p.pred) ? 0u : (uint32_t)p.pred[tile];
+        pk = tile == 0 ? p.entry0 : !p.pred ? 0u : (uint32_t)p.pred[tile];
         if (pk >= (uint32_t)NS && pk != kAllStates) pk = 0;
     }
     if (SPEC && pk == kAllStates) {
         // no assumption: count under every entry state, as the plain scan does
 #pragma unroll
-        for (int e = 0; e < NS; e++) L.cv[e] = thread_counts<D, false>(L.m, L.ls, L.prev_nl, e, L.base_t, len);
+        for (int e = 0; e < NS; e++) L.cv[e] = thread_counts<D, CROWS>(L.m, L.ls, L.prev_nl, e, L.base_t, len, prev_of(p));
     }
     if (SPEC && pk != kAllStates) {
         const uint32_t s_in = fapply(L.excl, pk);
@@ -217,7 +218,7 @@ __device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t
     const uint64_t t0 = globaltimer_ns();
     unknown = false;
     if (tile == 0) {
-        entry = 0;
+        entry = p.entry0;
         pre[0] = pre[1] = pre[2] = 0;
         return;
     }
@@ -318,7 +319,7 @@ __device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t
             const bool at_start = hi - kThreads < 0;
             S.lb_stop = found || at_start;
             if (found || at_start) {
-                const uint32_t ex = found ? S.lb_entry : 0u;
+                const uint32_t ex = found ? S.lb_entry : p.entry0;
                 uint32_t c0 = ac[0][0], c1 = ac[0][1], c2 = ac[0][2];
 #pragma unroll
                 for (int t = 1; t < NS; t++)
@@ -456,7 +457,7 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
     if (p.index) {
         for (uint32_t i = tid; i < n_tile; i += kThreads) {
             const uint64_t g = (uint64_t)pre[0] + i;
-            if (g < p.index_cap) p.index[g] = (uint32_t)(vs + S.stage[i]);
+            if (g < p.index_cap) p.index[g] = (uint32_t)(p.pos_base + vs + S.stage[i]);
         }
     }
     if (p.seps || p.ends) {
@@ -466,9 +467,9 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
         uint64_t mm = stm;
         while (mm) {
             const unsigned bpos = __ffsll((long long)mm) - 1;
-            const uint64_t pos = (uint64_t)(L.base_t + bpos);
+            const uint64_t pos = (uint64_t)(p.pos_base + L.base_t + bpos);
             if ((term >> bpos) & 1) {
-                if (p.ends && term_before < p.ends_cap) p.ends[term_before] = (sep_before << 32) | pos;
+                if (p.ends && term_before < p.ends_cap) p.ends[term_before] = ((p.sep_base + sep_before) << 32) | pos;
                 term_before++;
             } else {
                 if (p.seps && sep_before < p.seps_cap) p.seps[sep_before] = (uint32_t)pos;
@@ -533,6 +534,93 @@ __global__ void __launch_bounds__(kThreads) index_kernel(const __grid_constant__
         prev = cur;
         prev_tile = tile;
         have_prev = true;
+    }
+}
+
+// ===========================================================================
+// Shard summaries (several GPUs over one file): every tile's aggregate
+// (transfer function, counts per entry state) from a local pass alone, then
+// their composition in tile order. Nothing waits on another CTA.
+// ===========================================================================
+struct ShardSummaryDev {
+    uint32_t func;
+    uint32_t pad;
+    unsigned long long counts[4][3];  // per entry state: structurals, terminators, rows
+};
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) summary_tiles_kernel(const __grid_constant__ Params p) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    SmemIx &S = *reinterpret_cast<SmemIx *>(smem_raw);
+    const int tid = threadIdx.x;
+    for (uint32_t tile = blockIdx.x; tile < p.num_tiles; tile += gridDim.x) {
+        // plain 16-byte loads of the bytes a bulk copy of the tile would bring
+        const uint8_t *lo_full = p.abase + (uint64_t)tile * kTile - kPre;
+        const uint8_t *lo = tile == 0 ? p.abase : lo_full;
+        const uint8_t *end16 = p.abase + ((p.shift + p.len + 15) & ~15ull);
+        const uint8_t *hi = lo_full + kPre + kTile;
+        if (hi > end16) hi = end16;
+        uint8_t *dst = S.buf[0];
+        const uint32_t first = (uint32_t)(lo - lo_full), n16 = (uint32_t)(hi - lo) / 16;
+        for (uint32_t i = tid; i < n16; i += kThreads)
+            *reinterpret_cast<uint4 *>(dst + first + 16 * i) = reinterpret_cast<const uint4 *>(lo)[i];
+        __syncthreads();
+        LocalState L;
+        local_pass<D, false, true>(p, S, tile, S.buf[0], L);
+        __syncthreads();
+    }
+}
+
+constexpr int kSumThreads = 256;
+
+// Compose the tile aggregates of one shard in order (one CTA): each thread
+// folds a run of tiles, thread 0 folds the runs.
+template <int NS>
+__global__ void __launch_bounds__(kSumThreads) summary_reduce(const TileStatus *status, uint32_t tiles,
+                                                       ShardSummaryDev *out) {
+    __shared__ uint32_t sf[kSumThreads];
+    __shared__ unsigned long long sc[kSumThreads][4][3];
+    const int t = threadIdx.x;
+    const uint32_t per = (tiles + kSumThreads - 1) / kSumThreads;
+    uint32_t f = kIdentity;
+    unsigned long long c[4][3] = {};
+    for (uint32_t j = t * per; j < tiles && j < (uint32_t)(t + 1) * per; j++) {
+        const uint32_t g = status[j].func;
+        unsigned long long r[4][3];
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++) {
+            const unsigned long long v = status[j].agg[fapply(f, s0)];
+#pragma unroll
+            for (int k = 0; k < 3; k++) r[s0][k] = c[s0][k] + cfield(v, k);
+        }
+#pragma unroll
+        for (int s0 = 0; s0 < NS; s0++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) c[s0][k] = r[s0][k];
+        f = fcompose(f, g);
+    }
+    sf[t] = f;
+#pragma unroll
+    for (int s0 = 0; s0 < 4; s0++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) sc[t][s0][k] = c[s0][k];
+    __syncthreads();
+    if (t == 0) {
+        uint32_t af = kIdentity;
+        unsigned long long ac[4][3] = {};
+        for (int i = 0; i < kSumThreads; i++) {
+            unsigned long long r[4][3];
+            for (int s0 = 0; s0 < NS; s0++) {
+                const uint32_t m = fapply(af, s0);
+                for (int k = 0; k < 3; k++) r[s0][k] = ac[s0][k] + sc[i][m][k];
+            }
+            for (int s0 = 0; s0 < NS; s0++)
+                for (int k = 0; k < 3; k++) ac[s0][k] = r[s0][k];
+            af = fcompose(af, sf[i]);
+        }
+        out->func = af;
+        for (int s0 = 0; s0 < 4; s0++)
+            for (int k = 0; k < 3; k++) out->counts[s0][k] = s0 < NS ? ac[s0][k] : 0ull;
     }
 }
 
@@ -894,6 +982,7 @@ void falx_destroy(falx_ctx *c) {
     if (c->nd_host) cudaFreeHost(c->nd_host);
     if (c->mlp_scratch) cudaFree(c->mlp_scratch);
     if (c->pred) cudaFree(c->pred);
+    if (c->summary_dev) cudaFree(c->summary_dev);
     delete c;
 }
 
@@ -1099,6 +1188,107 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     host_out->n_seps = d.n_seps;
     host_out->n_ends = d.n_ends;
     return r2 ? r2 : rc;
+}
+
+// ---------------------------------------------------------------------------
+// Shards of one file (one per GPU): summary, then a seeded pass.
+// ---------------------------------------------------------------------------
+int falx_summarize_shard(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, int prev_byte,
+                       falx_shard_summary *out) {
+    int rc = check_common(c, dialect, data, len);
+    if (rc) return rc;
+    if (!out || prev_byte > 255) return FALX_ERR_INVALID;
+    memset(out, 0, sizeof *out);
+    static const uint32_t ns[5] = {2, 3, 1, 4, 4};
+    out->states = ns[dialect];
+    out->last_byte = -1;
+    for (uint32_t s0 = 0; s0 < 4; s0++) out->exit[s0] = s0;
+    if (len == 0) return FALX_OK;  // an empty shard passes every state through and counts nothing
+    const uint64_t shift = (uint64_t)((uintptr_t)data & 15u);
+    const uint32_t tiles = (uint32_t)((len + shift + kTile - 1) / kTile);
+    rc = ensure_status(c, tiles);
+    if (rc) return rc;
+    if (!c->summary_dev) FALX_CUDA(cudaMalloc(&c->summary_dev, sizeof(ShardSummaryDev)));
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.data = data;
+    P.abase = data - shift;
+    P.len = len;
+    P.shift = (uint32_t)shift;
+    P.num_tiles = tiles;
+    P.epoch = c->epoch;
+    P.status = c->status;
+    P.hdr = c->hdr;
+    P.seeded = prev_byte >= 0;
+    P.prev_byte = prev_byte >= 0 ? (uint32_t)prev_byte : 0u;
+    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)c->sm_count * 2);
+    ShardSummaryDev *sd = static_cast<ShardSummaryDev *>(c->summary_dev);
+#define FALX_SUMMARY(D)                                                                                     \
+    do {                                                                                                    \
+        FALX_CUDA(cudaFuncSetAttribute((const void *)summary_tiles_kernel<D>,                               \
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemIx)));  \
+        summary_tiles_kernel<D><<<grid, kThreads, sizeof(SmemIx), c->stream>>>(P);                          \
+        summary_reduce<NStates<D>::value><<<1, kSumThreads, 0, c->stream>>>(c->status, tiles, sd);           \
+    } while (0)
+    switch (dialect) {
+    case FALX_CSV: FALX_SUMMARY(D_CSV); break;
+    case FALX_CSV_HASH: FALX_SUMMARY(D_CSV_HASH); break;
+    case FALX_TSV: FALX_SUMMARY(D_TSV); break;
+    case FALX_LOGFMT: FALX_SUMMARY(D_LOGFMT); break;
+    default: FALX_SUMMARY(D_NDJSON); break;
+    }
+#undef FALX_SUMMARY
+    FALX_CUDA(cudaGetLastError());
+    ShardSummaryDev h;
+    uint8_t last = 0;
+    FALX_CUDA(cudaMemcpyAsync(&h, sd, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaMemcpyAsync(&last, data + len - 1, 1, cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    for (uint32_t s0 = 0; s0 < out->states; s0++) {
+        out->exit[s0] = (h.func >> (2 * s0)) & 3u;
+        out->structurals[s0] = h.counts[s0][0];
+        out->terminators[s0] = h.counts[s0][1];
+        out->rows[s0] = h.counts[s0][2];
+    }
+    out->last_byte = last;
+    return FALX_OK;
+}
+
+int falx_parse_tape_seeded(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, int prev_byte,
+                           uint32_t entry_state, uint64_t pos_base, uint64_t sep_base, uint32_t *index,
+                           uint64_t index_cap, uint32_t *seps, uint64_t seps_cap, uint64_t *ends, uint64_t ends_cap,
+                           uint64_t *n_index, uint64_t *n_seps, uint64_t *n_ends) {
+    int rc = check_common(c, dialect, data, len);
+    if (rc) return rc;
+    static const uint32_t ns[5] = {2, 3, 1, 4, 4};
+    if (prev_byte > 255 || entry_state >= ns[dialect] || pos_base + len > (1ull << 32)) return FALX_ERR_INVALID;
+    if ((index_cap && !index) || (seps_cap && !seps) || (ends_cap && !ends)) return FALX_ERR_INVALID;
+    uint64_t ni = 0, nt = 0;
+    if (len) {
+        Params P;
+        memset(&P, 0, sizeof P);
+        P.index = index_cap ? index : nullptr;
+        P.index_cap = index_cap;
+        P.seps = seps_cap ? seps : nullptr;
+        P.seps_cap = seps_cap;
+        P.ends = ends_cap ? ends : nullptr;
+        P.ends_cap = ends_cap;
+        P.seeded = prev_byte >= 0;
+        P.prev_byte = prev_byte >= 0 ? (uint32_t)prev_byte : 0u;
+        P.entry0 = entry_state;
+        P.pos_base = pos_base;
+        P.sep_base = sep_base;
+        rc = run_scan(c, dialect, false, data, len, P);
+        if (rc) return rc;
+        ni = c->hhdr->n_struct;
+        nt = c->hhdr->n_terms;
+    }
+    if (n_index) *n_index = ni;
+    if (n_seps) *n_seps = ni - nt;
+    if (n_ends) *n_ends = nt;
+    if ((index_cap && ni > index_cap) || (seps_cap && ni - nt > seps_cap) || (ends_cap && nt > ends_cap))
+        return FALX_ERR_CAPACITY;
+    return FALX_OK;
 }
 
 }  // extern "C"

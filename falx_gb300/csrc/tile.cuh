@@ -69,6 +69,14 @@ struct Params {
     uint64_t *ends;
     uint64_t ends_cap;
     int32_t dialect;       // batched launches: the document's dialect
+    // Seeded launches over one shard of a file: the automaton state and the
+    // byte before the shard, and what to add to output positions and to the
+    // separator counts of tape ends. Zero: the data is a whole file.
+    uint32_t seeded;
+    uint32_t prev_byte;
+    uint32_t entry0;
+    uint64_t pos_base;
+    uint64_t sep_base;
     const uint8_t *pred;   // speculative index: assumed entry state of every tile
     uint8_t *states64;     // optional: entry state of every 64-byte block
     RowSpec rows;
@@ -342,21 +350,34 @@ __device__ uint32_t lookback(const Params &p, uint32_t tile, int lane, uint32_t 
             return fapply(af, ex);
         }
     }
-    // reached the first tile: the file starts outside every region
-    pre[0] = ac[0][0];
-    pre[1] = ac[0][1];
-    pre[2] = ac[0][2];
-    return fapply(af, 0);
+    // reached the first tile: a file starts outside every region, a shard
+    // in its seed state
+    const uint32_t e0 = p.entry0;
+    uint32_t c0 = ac[0][0], c1 = ac[0][1], c2 = ac[0][2];
+#pragma unroll
+    for (int t = 1; t < NS; t++)
+        if (e0 == (uint32_t)t) { c0 = ac[t][0]; c1 = ac[t][1]; c2 = ac[t][2]; }
+    pre[0] = c0;
+    pre[1] = c1;
+    pre[2] = c2;
+    return fapply(af, e0);
 }
 
-// Record starts among this thread's 64 bytes for entry state s_in: file
-// position 0 and every byte after a structural newline, inside the file;
-// csv_hash records opening with '#' are comments, not rows.
+// The byte before position 0 of a launch: -1 at the start of a file.
+__device__ __forceinline__ int prev_of(const Params &p) { return p.seeded ? (int)p.prev_byte : -1; }
+// Position 0 starts a line: at a file start, or after a '\n'.
+__device__ __forceinline__ bool starts_line(int prev) { return prev < 0 || prev == '\n'; }
+
+// Record starts among this thread's 64 bytes for entry state s_in: position
+// 0 (at a file start, or after a structural newline before a shard) and
+// every byte after a structural newline, inside the data; csv_hash records
+// opening with '#' are comments, not rows.
 template <int D>
 __device__ __forceinline__ uint64_t row_starts(const Masks &m, uint64_t term, bool prev_nl, uint32_t s_in,
-                                               int64_t base_t, int64_t len) {
+                                               int64_t base_t, int64_t len, int prev) {
     uint64_t rs = (term << 1) | (uint64_t)(prev_nl && state_outside<D>(s_in));
-    if (base_t <= 0 && base_t + kThreadBytes > 0) rs |= 1ull << (-base_t);
+    if (base_t <= 0 && base_t + kThreadBytes > 0 && (prev < 0 || (prev == '\n' && state_outside<D>(s_in))))
+        rs |= 1ull << (-base_t);
     const int64_t live = len - base_t;
     if (live < kThreadBytes) rs &= live <= 0 ? 0 : ((1ull << live) - 1);
     if (base_t < 0) rs &= ~((1ull << (-base_t)) - 1);
@@ -366,11 +387,11 @@ __device__ __forceinline__ uint64_t row_starts(const Masks &m, uint64_t term, bo
 
 template <int D, bool ROWS>
 __device__ __forceinline__ unsigned long long thread_counts(const Masks &m, uint64_t ls, bool prev_nl, uint32_t s,
-                                                            int64_t base_t, int64_t len) {
+                                                            int64_t base_t, int64_t len, int prev) {
     const uint64_t st = structural_mask<D>(m, ls, s);
     const uint64_t term = st & m.nl;
     unsigned long long c = (unsigned long long)__popcll(st) | ((unsigned long long)__popcll(term) << 21);
-    if (ROWS) c |= (unsigned long long)__popcll(row_starts<D>(m, term, prev_nl, s, base_t, len)) << 42;
+    if (ROWS) c |= (unsigned long long)__popcll(row_starts<D>(m, term, prev_nl, s, base_t, len, prev)) << 42;
     return c;
 }
 
@@ -403,7 +424,7 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS, NB> &S,
     const int64_t base_t = vs + (int64_t)tid * kThreadBytes;
     const bool prev_nl = b[kPre + tid * kThreadBytes - 1] == '\n';
     uint64_t ls = (m.nl << 1) | (uint64_t)prev_nl;
-    if (base_t <= 0 && base_t + kThreadBytes > 0) ls |= 1ull << (-base_t);
+    if (base_t <= 0 && base_t + kThreadBytes > 0 && starts_line(prev_of(p))) ls |= 1ull << (-base_t);
 
     // ---- transfer functions: thread -> warp -> block
     const uint32_t f = thread_function<D>(m, ls);
@@ -427,7 +448,7 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS, NB> &S,
     constexpr int NS = NStates<D>::value;
     unsigned long long cv[NS];
 #pragma unroll
-    for (int e = 0; e < NS; e++) cv[e] = thread_counts<D, ROWS>(m, ls, prev_nl, e, base_t, len);
+    for (int e = 0; e < NS; e++) cv[e] = thread_counts<D, ROWS>(m, ls, prev_nl, e, base_t, len, prev_of(p));
     {
         unsigned long long v[NS];
 #pragma unroll
@@ -489,7 +510,7 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS, NB> &S,
     const uint64_t stm = structural_mask<D>(m, ls, s_in);
     const uint64_t term = stm & m.nl;
     uint64_t rows_m = 0;
-    if (ROWS) rows_m = row_starts<D>(m, term, prev_nl, s_in, base_t, len);
+    if (ROWS) rows_m = row_starts<D>(m, term, prev_nl, s_in, base_t, len, prev_of(p));
     unsigned long long c = cv[0];
 #pragma unroll
     for (int t = 1; t < NS; t++) c = s_in == (uint32_t)t ? cv[t] : c;
@@ -527,14 +548,14 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS, NB> &S,
     if (p.index && !overflow) {
         for (uint32_t i = tid; i < n_tile; i += kThreads) {
             uint64_t g = (uint64_t)sbase + i;
-            if (g < p.index_cap) p.index[g] = (uint32_t)(vs + (S.stage[i] & 0x7FFF));
+            if (g < p.index_cap) p.index[g] = (uint32_t)(p.pos_base + vs + (S.stage[i] & 0x7FFF));
         }
     } else if (p.index) {
         uint64_t g = (uint64_t)sbase + cfield(ce, 0);
         uint64_t mm = stm;
         while (mm) {
             const unsigned bpos = __ffsll((long long)mm) - 1;
-            if (g < p.index_cap) p.index[g] = (uint32_t)(base_t + bpos);
+            if (g < p.index_cap) p.index[g] = (uint32_t)(p.pos_base + base_t + bpos);
             g++;
             mm &= mm - 1;
         }
@@ -548,9 +569,9 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS, NB> &S,
         uint64_t mm = stm;
         while (mm) {
             unsigned bpos = __ffsll((long long)mm) - 1;
-            uint64_t pos = (uint64_t)(base_t + bpos);
+            uint64_t pos = (uint64_t)(p.pos_base + base_t + bpos);
             if ((term >> bpos) & 1) {
-                if (p.ends && term_before < p.ends_cap) p.ends[term_before] = (sep_before << 32) | pos;
+                if (p.ends && term_before < p.ends_cap) p.ends[term_before] = ((p.sep_base + sep_before) << 32) | pos;
                 term_before++;
             } else {
                 if (p.seps && sep_before < p.seps_cap) p.seps[sep_before] = (uint32_t)pos;

@@ -182,6 +182,38 @@ int falx_parse_host(falx_ctx *ctx, const falx_schema *schema, const uint8_t *hos
                     falx_outputs *host_out);
 
 /* ---------------------------------------------------------------------------
+ * Shards of one file on several GPUs (one process per GPU). Each rank
+ * summarises its shard independently of the state it starts in, the ranks
+ * exchange the summaries (a few dozen bytes each, through the host), every
+ * rank folds the summaries of the ranks before it into its true entry state
+ * and output offsets, then runs a seeded pass that writes its own range of
+ * the global index / tape. The reference runs the same three steps across
+ * threads (csv_hash.rs:152-214 region_scan3 phases; csv_geo.rs:95-149
+ * chunk parities; seeded pass index_structurals_seeded, csv_geo.rs:1855-1873).
+ * `prev_byte` is the byte before the shard (-1 at the start of the file); it
+ * decides whether the shard starts a line (csv_hash comments) and a record.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    uint32_t states;          /* entry states of the dialect's automaton */
+    uint32_t exit[4];         /* exit state for each entry state */
+    uint64_t structurals[4];  /* counts for each entry state */
+    uint64_t terminators[4];
+    uint64_t rows[4];         /* record starts inside the shard (csv_hash comments excluded) */
+    int32_t last_byte;        /* the shard's last byte, -1 if empty */
+} falx_shard_summary;
+
+int falx_summarize_shard(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len, int prev_byte,
+                       falx_shard_summary *out);
+/* Seeded pass: structural index and / or tape of the shard as part of the
+ * whole file. Positions get pos_base (the shard's file offset) added, tape
+ * ends count separators from sep_base; entry_state comes from the summaries
+ * of the shards before it. NULL / zero-capacity outputs are skipped. */
+int falx_parse_tape_seeded(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len, int prev_byte,
+                           uint32_t entry_state, uint64_t pos_base, uint64_t sep_base, uint32_t *index,
+                           uint64_t index_cap, uint32_t *seps, uint64_t seps_cap, uint64_t *ends, uint64_t ends_cap,
+                           uint64_t *n_index, uint64_t *n_seps, uint64_t *n_ends);
+
+/* ---------------------------------------------------------------------------
  * Learned speculation. The reference's parallel drivers guess each chunk's
  * entry state ("outside quotes") and re-index chunks whose guess was wrong
  * (csv_geo.rs:95-149 speculative parity; csv_hash.rs:152-214 instead runs a

@@ -43,6 +43,9 @@ def lib():
         l = ctypes.CDLL(_build.build())
         l.orc_index_spec.restype = c_uint64
         l.orc_index_spec.argtypes = [c_int, c_void_p, c_uint64, c_void_p, c_uint64]
+        l.orc_index_seeded.restype = c_uint64
+        l.orc_index_seeded.argtypes = [c_int, c_void_p, c_uint64, c_uint32, c_int, c_uint64, c_void_p, c_uint64,
+                                       POINTER(c_uint32), POINTER(c_uint64), POINTER(c_uint64)]
         l.orc_index_blocks.restype = c_uint64
         l.orc_index_blocks.argtypes = [c_int, c_void_p, c_uint64, c_void_p, c_uint64]
         l.orc_parse_tape.restype = None
@@ -87,6 +90,30 @@ def index_spec(data, dialect):
     out = np.zeros(max(cnt, 1), dtype=np.uint32)
     lib().orc_index_spec(dialect, p, n, out.ctypes.data_as(c_void_p), cnt)
     return out[:cnt]
+
+
+NSTATES = {CSV: 2, CSV_HASH: 3, TSV: 1, LOGFMT: 4, NDJSON: 4}
+
+
+def index_seeded(data, dialect, state=0, prev_byte=-1, pos_base=0):
+    """Seeded serial pass over a shard: (index, exit state, terminators, rows)."""
+    a, p, n = _buf(data)
+    ex, t, r = c_uint32(), c_uint64(), c_uint64()
+    cnt = lib().orc_index_seeded(dialect, p, n, state, prev_byte, pos_base, None, 0, byref(ex), byref(t), byref(r))
+    out = np.zeros(max(cnt, 1), dtype=np.uint32)
+    lib().orc_index_seeded(dialect, p, n, state, prev_byte, pos_base, out.ctypes.data_as(c_void_p), cnt, byref(ex),
+                           byref(t), byref(r))
+    return out[:cnt], ex.value, t.value, r.value
+
+
+def shard_summary(data, dialect, prev_byte=-1):
+    """Entry-independent summary of a shard: per entry state its exit state
+    and its structural / terminator / row counts."""
+    out = []
+    for s in range(NSTATES[dialect]):
+        idx, ex, t, r = index_seeded(data, dialect, s, prev_byte)
+        out.append({"exit": ex, "structurals": int(idx.size), "terminators": t, "rows": r})
+    return out
 
 
 def index_blocks(data, dialect):

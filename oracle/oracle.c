@@ -73,6 +73,76 @@ uint64_t orc_index_spec(int dialect, const uint8_t *d, uint64_t n, uint32_t *out
     return cnt;
 }
 
+/* Seeded serial pass over one shard of a file (index_structurals_seeded,
+ * csv_geo.rs:1855-1873; csv_hash seeds `line_start | region << 1`,
+ * csv_hash.rs:1877, codegen.rs:1097-1106). `state` is the automaton state
+ * before the shard in the engine's encoding (csv: in quotes; csv_hash: 0
+ * normal, 1 quote, 2 comment; logfmt / ndjson: escape carry | quote parity
+ * << 1), `prev_byte` the byte before it (-1: file start). Positions are
+ * written plus pos_base. Returns the structural count; reports the exit
+ * state, terminators and rows (record starts inside the shard, csv_hash
+ * comment records excluded). */
+uint64_t orc_index_seeded(int dialect, const uint8_t *d, uint64_t n, uint32_t state, int prev_byte,
+                          uint64_t pos_base, uint32_t *out, uint64_t cap, uint32_t *exit_state, uint64_t *terms,
+                          uint64_t *rows) {
+    orc_dialect dl = dialect_of(dialect);
+    int in_quotes, in_comment = 0;
+    uint64_t escape_run = 0, cnt = 0, nterm = 0, nrows = 0;
+    if (dialect == 1) {
+        in_quotes = state == 1;
+        in_comment = state == 2;
+    } else if (dialect == 3 || dialect == 4) {
+        escape_run = state & 1;
+        in_quotes = (state >> 1) & 1;
+    } else {
+        in_quotes = (int)(state & 1);
+    }
+    int line_start = prev_byte < 0 || prev_byte == '\n';
+    /* position 0 starts a record at the file start, or after a structural newline */
+    int rec = prev_byte < 0 || (prev_byte == '\n' && !in_quotes && !in_comment);
+    for (uint64_t i = 0; i < n; i++) {
+        uint8_t b = d[i];
+        if (rec) {
+            if (!(dialect == 1 && b == '#')) nrows++;
+            rec = 0;
+        }
+        int escaped = (escape_run & 1) == 1;
+        if (dl.escape >= 0 && b == (uint8_t)dl.escape) escape_run++;
+        else escape_run = 0;
+        int st = 0;
+        if (in_comment) {
+            if (b == '\n') {
+                in_comment = 0;
+                st = in_set(dl.structural, '\n');
+            }
+        } else if (dl.quote >= 0 && b == (uint8_t)dl.quote) {
+            if (!escaped) in_quotes = !in_quotes;
+        } else if (!in_quotes && dl.comment >= 0 && b == (uint8_t)dl.comment && line_start) {
+            in_comment = 1;
+        } else if (!in_quotes && in_set(dl.structural, b)) {
+            st = 1;
+        }
+        if (st) {
+            if (cnt < cap) out[cnt] = (uint32_t)(pos_base + i);
+            cnt++;
+            if (b == '\n') {
+                nterm++;
+                rec = 1;
+            }
+        }
+        line_start = b == '\n';
+    }
+    if (exit_state) {
+        if (dialect == 1) *exit_state = in_comment ? 2u : in_quotes ? 1u : 0u;
+        else if (dialect == 3 || dialect == 4) *exit_state = (uint32_t)((escape_run & 1) | ((uint64_t)in_quotes << 1));
+        else if (dialect == 2) *exit_state = 0;
+        else *exit_state = (uint32_t)in_quotes;
+    }
+    if (terms) *terms = nterm;
+    if (rows) *rows = nrows;
+    return cnt;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Blockwise restatement of the generated `step` functions.                   */
 /* ------------------------------------------------------------------------- */

@@ -33,6 +33,9 @@ enum { ORC_I64 = 0, ORC_U32 = 1, ORC_F64 = 2, ORC_STR = 3, ORC_BYTES = 4 };
 /* Byte-serial structural index (src/scalar.rs:23-59). Returns the number of
  * structurals; writes at most `cap` of them. */
 uint64_t orc_index_spec(int dialect, const uint8_t *d, uint64_t n, uint32_t *out, uint64_t cap);
+uint64_t orc_index_seeded(int dialect, const uint8_t *d, uint64_t n, uint32_t state, int prev_byte,
+                          uint64_t pos_base, uint32_t *out, uint64_t cap, uint32_t *exit_state, uint64_t *terms,
+                          uint64_t *rows);
 
 /* Blockwise restatement of the generated `step` kernels: 64-byte blocks,
  * zero-padded tail, carried state between blocks (csv_geo.rs:2117-2127,
