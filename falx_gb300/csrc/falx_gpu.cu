@@ -574,10 +574,13 @@ __global__ void __launch_bounds__(kThreads) summary_tiles_kernel(const __grid_co
 constexpr int kSumThreads = 256;
 
 // Compose the tile aggregates of one shard in order (one CTA): each thread
-// folds a run of tiles, thread 0 folds the runs.
+// folds a run of tiles, thread 0 folds the runs. With backslash escapes
+// (NS == 4) the tiles' functions carry the escape bit through the zero
+// padding after the last byte, which consumes it; the shard's exit escape
+// bit comes from its trailing run of backslashes instead.
 template <int NS>
 __global__ void __launch_bounds__(kSumThreads) summary_reduce(const TileStatus *status, uint32_t tiles,
-                                                       ShardSummaryDev *out) {
+                                                       const uint8_t *data, uint64_t len, ShardSummaryDev *out) {
     __shared__ uint32_t sf[kSumThreads];
     __shared__ unsigned long long sc[kSumThreads][4][3];
     const int t = threadIdx.x;
@@ -617,6 +620,16 @@ __global__ void __launch_bounds__(kSumThreads) summary_reduce(const TileStatus *
             for (int s0 = 0; s0 < NS; s0++)
                 for (int k = 0; k < 3; k++) ac[s0][k] = r[s0][k];
             af = fcompose(af, sf[i]);
+        }
+        if (NS == 4) {
+            uint64_t k = 0;
+            while (k < len && data[len - 1 - k] == '\\') k++;
+            uint32_t fixed = 0;
+            for (uint32_t s0 = 0; s0 < 4; s0++) {
+                const uint32_t esc = k < len ? (uint32_t)(k & 1) : (uint32_t)((len + (s0 & 1)) & 1);
+                fixed |= ((fapply(af, s0) & 2u) | esc) << (2 * s0);
+            }
+            af = fixed;
         }
         out->func = af;
         for (int s0 = 0; s0 < 4; s0++)
@@ -1228,7 +1241,7 @@ int falx_summarize_shard(falx_ctx *c, int dialect, const uint8_t *data, uint64_t
         FALX_CUDA(cudaFuncSetAttribute((const void *)summary_tiles_kernel<D>,                               \
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemIx)));  \
         summary_tiles_kernel<D><<<grid, kThreads, sizeof(SmemIx), c->stream>>>(P);                          \
-        summary_reduce<NStates<D>::value><<<1, kSumThreads, 0, c->stream>>>(c->status, tiles, sd);           \
+        summary_reduce<NStates<D>::value><<<1, kSumThreads, 0, c->stream>>>(c->status, tiles, data, len, sd); \
     } while (0)
     switch (dialect) {
     case FALX_CSV: FALX_SUMMARY(D_CSV); break;
