@@ -86,6 +86,7 @@ SIGNATURES = {
     "falx_create": (c_int, [c_int, POINTER(c_void_p)]),
     "falx_destroy": (None, [c_void_p]),
     "falx_set_stream": (c_int, [c_void_p, c_void_p]),
+    "falx_set_option": (c_int, [c_void_p, c_int, c_int]),
     "falx_strerror": (c_char_p, [c_int]),
     "falx_index_structurals": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64)]),
     "falx_parse_tape": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, c_void_p, c_uint64,
@@ -133,6 +134,8 @@ SIGNATURES = {
     "falx_batch_plan": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_uint32, POINTER(c_uint32)]),
 }
 
+OPT_ROWS_PATH = 1
+OPT_CTAS_PER_SM = 2
 MLP_BYTES = 256
 SPEC_TILE = 16384
 

@@ -54,7 +54,7 @@ __device__ __forceinline__ void batch_tile(const Params &p, Smem<true, NB> &S, u
 }
 
 template <int NB>
-__global__ void __launch_bounds__(kThreads) batch_kernel(const Params *docs, const BatchItem *items,
+__global__ void __launch_bounds__(kThreads, 3) batch_kernel(const Params *docs, const BatchItem *items,
                                                          uint32_t n_items, uint32_t *ticket) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     BatchSmem<NB> &B = *reinterpret_cast<BatchSmem<NB> *>(smem_raw);

@@ -48,4 +48,12 @@ struct falx_ctx {
     uint64_t pred_cap = 0;
     falx_batch_tuning batch_tuned;  // last autotuned batched-launch configuration
     void *summary_dev = nullptr;    // shard summary result (device)
+    // rows from the tape: scratch tape, per-record-block sums
+    int rows_path = 0;              // 0: index + tape, then columns_kernel; 1: fused tile pass
+    uint32_t *tape_seps = nullptr;
+    uint64_t tape_seps_cap = 0;     // bytes
+    uint64_t *tape_ends = nullptr;
+    uint64_t tape_ends_cap = 0;     // bytes
+    void *rec_sums = nullptr;
+    uint64_t rec_sums_cap = 0;      // bytes
 };

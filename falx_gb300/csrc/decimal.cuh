@@ -353,8 +353,10 @@ FALX_HD bool parse_f64(const uint8_t *s, uint32_t len, double &out) {
             m = m * 10 + c;
         }
         if (ok) {
-            double v = (double)m / 1e6;
-            out = u2d(d2u(v) | ((uint64_t)neg << 63));
+            // m / 1e6 correctly rounded, as the reference's IEEE division
+            // gives it; Eisel-Lemire is exact for decimal exponents in
+            // [-27, 55] and needs no floating-point unit
+            out = u2d(eisel_lemire(m, -6) | ((uint64_t)neg << 63));
             return true;
         }
     }
@@ -421,11 +423,9 @@ FALX_HD bool parse_f64(const uint8_t *s, uint32_t len, double &out) {
     uint64_t bits;
     if (w == 0) {
         bits = 0;
-    } else if (!trunc && w <= (1ull << 53) && e10 >= -22 && e10 <= 22) {
-        const double p10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
-                                1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
-        double v = e10 < 0 ? (double)w / p10[-e10] : (double)w * p10[e10];
-        bits = d2u(v);
+    } else if (!trunc && e10 >= -27 && e10 <= 55) {
+        // exact 128-bit product range (covers Clinger's exact doubles too)
+        bits = eisel_lemire(w, e10);
     } else if (!trunc) {
         bits = eisel_lemire(w, e10);
     } else {
@@ -464,14 +464,22 @@ FALX_HD bool parse_u32(const uint8_t *s, uint32_t len, uint32_t &out) {
         if (len == 1) return false;
         i = 1;
     }
-    uint64_t v = 0;
-    for (; i < len; i++) {
-        uint32_t d = (uint8_t)(s[i] - '0');
+    // nine digits fit 32 bits; a tenth is checked in 64
+    uint32_t v = 0;
+    const uint32_t end9 = len - i > 9 ? i + 9 : len;
+    for (; i < end9; i++) {
+        const uint32_t d = (uint8_t)(s[i] - '0');
         if (d >= 10) return false;
         v = v * 10 + d;
-        if (v > 0xFFFFFFFFull) return false;
     }
-    out = (uint32_t)v;
+    uint64_t w = v;
+    for (; i < len; i++) {
+        const uint32_t d = (uint8_t)(s[i] - '0');
+        if (d >= 10) return false;
+        w = w * 10 + d;
+        if (w > 0xFFFFFFFFull) return false;
+    }
+    out = (uint32_t)w;
     return true;
 }
 

@@ -33,6 +33,7 @@
 #include "scan_core.cuh"
 
 #include "tile.cuh"
+#include "columns.cuh"
 
 namespace falx {
 
@@ -65,16 +66,12 @@ struct SmemIx {
     unsigned long long warp_c[kWarps];
     uint32_t tile_f, ptile_f;
     unsigned long long agg[4], pagg[4];
-    // block-wide look-back
-    uint32_t lb_wf[kWarps];
-    unsigned long long lb_wc[kWarps][4];
-    uint32_t lb_first_incl[3], lb_first_wait[3], lb_stop, lb_entry, lb_pre[3];
+    LookbackSmem lb;  // block-wide look-back
     uint32_t base[3];
     unsigned long long tile_c;
     // speculative index: entry state assumed by the tile in its local pass
     // and by the deferred one; counts of the look-back not known yet
     uint32_t spec_p, pspec_p;
-    uint32_t lb_restart;
 };
 
 // Local pass of one tile: classify, scan transfer functions, publish the
@@ -194,153 +191,6 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
     }
 }
 
-// Block-wide look-back (all threads): thread t watches predecessor
-// tile - 1 - t. Waits only for the predecessors nearer than the nearest
-// published inclusive prefix (level kIncl); returns the tile's entry state,
-// the counts of the file before it and, for speculative aggregates, whether
-// some of those counts are not known yet.
-//
-// Speculative status levels: 1 = the tile's full transfer function, the
-// entry state it assumed and its counts under that assumption; 2 = its true
-// exit state and its counts under its true entry (published by a tile whose
-// assumption was wrong, as soon as its look-back knows its entry); 3 = its
-// inclusive prefix. The entry state never waits on counts: it follows from
-// the transfer functions alone. A level-1 tile that assumed the wrong entry
-// makes the counts unknown until it reaches level 2.
-template <int NS, bool SPEC>
-__device__ void lookback_cta(const Params &p, SmemIx &S, uint32_t tile, uint32_t &entry, uint32_t pre[3],
-                             bool &unknown) {
-    constexpr uint32_t kIncl = SPEC ? 3 : 2;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    uint32_t af = kIdentity;  // thread 0: aggregate between the window and `tile`
-    uint32_t ac[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    uint32_t au = 0;
-    const uint64_t t0 = globaltimer_ns();
-    unknown = false;
-    if (tile == 0) {
-        entry = p.entry0;
-        pre[0] = pre[1] = pre[2] = 0;
-        return;
-    }
-    for (int64_t hi = (int64_t)tile - 1; hi >= 0; hi -= kThreads) {
-        const int64_t j = hi - tid;
-        const bool in = j >= 0;
-        uint32_t flag = 0;
-        uint32_t sidx;
-        // Three rotating slots for the block-wide minima: in poll iteration
-        // `it` thread 0 resets slot it+1 before the barrier, every thread
-        // updates slot it before it and reads slot it after it. No slot is
-        // reset while a thread may still read it.
-        if (tid == 0) {
-            S.lb_first_incl[0] = S.lb_first_wait[0] = kThreads;
-        }
-        __syncthreads();
-        for (uint32_t it = 0;; it++) {
-            const uint32_t sl = it % 3, nx = (it + 1) % 3;
-            if (tid == 0) S.lb_first_incl[nx] = S.lb_first_wait[nx] = kThreads;
-            if (in) flag = ld_acquire(&p.status[j].flag);
-            const bool cur = (flag >> 2) == p.epoch;
-            const bool waitv = in && !(cur && (flag & 3) >= 1);
-            const bool incl = in && cur && (flag & 3) >= kIncl;
-            const uint32_t bw = __ballot_sync(0xffffffffu, waitv), bi = __ballot_sync(0xffffffffu, incl);
-            if (lane == 0 && bw) atomicMin(&S.lb_first_wait[sl], (uint32_t)(warp * 32 + __ffs(bw) - 1));
-            if (lane == 0 && bi) atomicMin(&S.lb_first_incl[sl], (uint32_t)(warp * 32 + __ffs(bi) - 1));
-            __syncthreads();
-            const uint32_t fw = S.lb_first_wait[sl], fi = S.lb_first_incl[sl];
-            sidx = fi;
-            if (fw > fi || fw == (uint32_t)kThreads) break;
-            if ((it & 15) == 15) {
-                const bool stop = tid == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
-                if (__syncthreads_or(stop)) {
-                    if (tid == 0) fail(p.hdr, ERR_TIMEOUT);
-                    entry = 0;
-                    pre[0] = pre[1] = pre[2] = 0;
-                    return;
-                }
-            }
-            __nanosleep(64);
-        }
-        uint32_t f = kIdentity;
-        uint64_t c[4] = {0, 0, 0, 0};
-        if (in && (uint32_t)tid < sidx) {
-            if (!SPEC) {
-                f = ld_relaxed(&p.status[j].func);
-#pragma unroll
-                for (int s0 = 0; s0 < NS; s0++) c[s0] = ld_relaxed64(&p.status[j].agg[s0]);
-            } else if ((flag & 3) >= 2) {
-                f = fconst(ld_relaxed(&p.status[j].exit));
-                const uint64_t v = ld_relaxed64(&p.status[j].agg[1]);
-#pragma unroll
-                for (int s0 = 0; s0 < NS; s0++) c[s0] = v;
-            } else {
-                const uint32_t pf = ld_relaxed(&p.status[j].func);
-                f = pf & 0xFF;
-                if ((pf >> 8) == kAllStates) {
-#pragma unroll
-                    for (int s0 = 0; s0 < NS; s0++) c[s0] = ld_relaxed64(&p.status[j].agg[s0]);
-                } else {
-                    const uint64_t v = ld_relaxed64(&p.status[j].agg[0]);
-#pragma unroll
-                    for (int s0 = 0; s0 < NS; s0++) c[s0] = (uint32_t)s0 == (pf >> 8) ? v : kUnknown;
-                }
-            }
-        }
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t gf = __shfl_down_sync(0xffffffffu, f, d);
-            uint64_t gc[4];
-#pragma unroll
-            for (int s0 = 0; s0 < NS; s0++) gc[s0] = __shfl_down_sync(0xffffffffu, c[s0], d);
-            if (lane + d < 32) {
-                if (SPEC) agg_prepend_spec<NS>(gf, gc, f, c);
-                else agg_prepend<NS>(gf, gc, f, c);
-            }
-        }
-        if (lane == 0) {
-            S.lb_wf[warp] = f;
-#pragma unroll
-            for (int s0 = 0; s0 < NS; s0++) S.lb_wc[warp][s0] = c[s0];
-        }
-        if ((uint32_t)tid == sidx) {
-            S.lb_entry = ld_relaxed(&p.status[j].exit);
-            S.lb_pre[0] = ld_relaxed(&p.status[j].incl[0]);
-            S.lb_pre[1] = ld_relaxed(&p.status[j].incl[1]);
-            S.lb_pre[2] = ld_relaxed(&p.status[j].incl[2]);
-        }
-        __syncthreads();
-        if (tid == 0) {
-            for (int w = 0; w < kWarps; w++) {
-                unsigned long long g[4];
-#pragma unroll
-                for (int s0 = 0; s0 < NS; s0++) g[s0] = S.lb_wc[w][s0];
-                wide_prepend<NS>(S.lb_wf[w], g, af, ac, au);
-            }
-            const bool found = sidx < (uint32_t)kThreads;
-            const bool at_start = hi - kThreads < 0;
-            S.lb_stop = found || at_start;
-            if (found || at_start) {
-                const uint32_t ex = found ? S.lb_entry : p.entry0;
-                uint32_t c0 = ac[0][0], c1 = ac[0][1], c2 = ac[0][2];
-#pragma unroll
-                for (int t = 1; t < NS; t++)
-                    if (ex == (uint32_t)t) { c0 = ac[t][0]; c1 = ac[t][1]; c2 = ac[t][2]; }
-                S.lb_pre[0] = (found ? S.lb_pre[0] : 0u) + c0;
-                S.lb_pre[1] = (found ? S.lb_pre[1] : 0u) + c1;
-                S.lb_pre[2] = (found ? S.lb_pre[2] : 0u) + c2;
-                S.lb_entry = fapply(af, ex);
-                S.lb_restart = (au >> ex) & 1u;
-            }
-        }
-        __syncthreads();
-        if (S.lb_stop) break;
-    }
-    entry = S.lb_entry;
-    pre[0] = S.lb_pre[0];
-    pre[1] = S.lb_pre[1];
-    pre[2] = S.lb_pre[2];
-    unknown = SPEC && S.lb_restart;
-}
-
 // Deferred output of one tile: inclusive prefix, staged index, tape.
 // SPEC: a tile whose true entry (from the look-back) equals the one it
 // assumed reuses its local-pass masks; otherwise it re-derives them from
@@ -354,7 +204,7 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
     const int64_t vs = (int64_t)tile * kTile - (int64_t)p.shift;
     uint32_t entry, pre[3];
     bool unknown;
-    lookback_cta<NS, SPEC>(p, S, tile, entry, pre, unknown);
+    lookback_cta<NS, SPEC>(p, S.lb, tile, entry, pre, unknown);
     const bool full = !SPEC || S.pspec_p == kAllStates;  // counted under every entry
     const bool hit = full || entry == S.pspec_p;         // block-uniform
     if (tid == 0 && hit && !unknown) {
@@ -423,7 +273,7 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
             }
             __nanosleep(128);
             uint32_t e2;
-            lookback_cta<NS, SPEC>(p, S, tile, e2, pre, unknown);
+            lookback_cta<NS, SPEC>(p, S.lb, tile, e2, pre, unknown);
         }
         if (tid == 0) {
             const unsigned long long mine = S.tile_c;
@@ -643,7 +493,7 @@ __global__ void __launch_bounds__(kSumThreads) summary_reduce(const TileStatus *
 // tiles of the same or an earlier round, which resident CTAs are already
 // processing. The bulk copy of a CTA's next tile is issued one round ahead.
 template <int D, bool ROWS>
-__global__ void __launch_bounds__(kThreads) scan_kernel(const __grid_constant__ Params p) {
+__global__ void __launch_bounds__(kThreads, 3) scan_kernel(const __grid_constant__ Params p) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     Smem<ROWS> &S = *reinterpret_cast<Smem<ROWS> *>(smem_raw);
     const int tid = threadIdx.x;
@@ -843,6 +693,102 @@ int validate_schema(const falx_schema *s, RowSpec &rs, uint64_t rows_cap, const 
     return FALX_OK;
 }
 
+// Grow a device scratch buffer to `need` bytes (contents not kept).
+int grow_scratch(void **p, uint64_t *cap, uint64_t need) {
+    if (need <= *cap) return FALX_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const uint64_t want = need + need / 8;
+    FALX_CUDA(cudaMalloc(p, want));
+    *cap = want;
+    return FALX_OK;
+}
+
+// Rows, field bytes and count / sum from the tape: the index kernel writes
+// the tape (the caller's buffers when they are large enough, else scratch),
+// then columns_kernel decodes the records. P carries the caller's index and
+// tape outputs; rs the columns and sinks.
+int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, Params P) {
+    uint32_t *seps = P.seps;
+    uint64_t *ends = P.ends;
+    uint64_t scap = P.seps_cap, ecap = P.ends_cap;
+    const bool own = !seps || !ends;
+    if (own) {
+        // first guess from the input size; grown and re-run if too small
+        uint64_t gs = (len / 6 + 1024) * 4, ge = (len / 24 + 1024) * 8;
+        if (c->tape_seps_cap > gs) gs = c->tape_seps_cap;
+        if (c->tape_ends_cap > ge) ge = c->tape_ends_cap;
+        int rc = grow_scratch((void **)&c->tape_seps, &c->tape_seps_cap, gs);
+        if (!rc) rc = grow_scratch((void **)&c->tape_ends, &c->tape_ends_cap, ge);
+        if (rc) return rc;
+        P.seps = c->tape_seps;
+        P.seps_cap = c->tape_seps_cap / 4;
+        P.ends = c->tape_ends;
+        P.ends_cap = c->tape_ends_cap / 8;
+    }
+    const RowSpec rs = P.rows;
+    memset(&P.rows, 0, sizeof P.rows);
+    int rc = run_scan(c, dialect, false, data, len, P);
+    if (rc) return rc;
+    uint64_t n_struct = c->hhdr->n_struct, n_terms = c->hhdr->n_terms;
+    if (n_struct - n_terms > P.seps_cap || n_terms > P.ends_cap) {
+        // the tape did not fit: index once more into scratch of the exact size
+        rc = grow_scratch((void **)&c->tape_seps, &c->tape_seps_cap, (n_struct - n_terms + 1) * 4);
+        if (!rc) rc = grow_scratch((void **)&c->tape_ends, &c->tape_ends_cap, (n_terms + 1) * 8);
+        if (rc) return rc;
+        P.index = nullptr;
+        P.index_cap = 0;
+        P.seps = c->tape_seps;
+        P.seps_cap = c->tape_seps_cap / 4;
+        P.ends = c->tape_ends;
+        P.ends_cap = c->tape_ends_cap / 8;
+        rc = run_scan(c, dialect, false, data, len, P);
+        if (rc) return rc;
+    }
+    ColParams cp;
+    memset(&cp, 0, sizeof cp);
+    cp.data = data;
+    cp.shift = (uint32_t)((uintptr_t)data & 15u);
+    cp.abase = data - cp.shift;
+    cp.len = len;
+    cp.seps = P.seps;
+    cp.n_seps = n_struct - n_terms;
+    cp.ends = P.ends;
+    cp.n_ends = n_terms;
+    cp.n_recs = n_terms + 1;
+    cp.hdr = c->hdr;
+    cp.rows = rs;
+    const uint64_t blocks = (cp.n_recs + kRecBlock - 1) / kRecBlock;
+    rc = grow_scratch(&c->rec_sums, &c->rec_sums_cap, blocks * sizeof(RecSums));
+    if (rc) return rc;
+    cp.sums = static_cast<RecSums *>(c->rec_sums);
+    // count rows and string bytes per block, scan, then decode
+    const size_t smem_cells = sizeof(ColSmem), smem_count = sizeof(ColSmem) - kDataWin;
+#define FALX_COLS(D)                                                                                           \
+    do {                                                                                                       \
+        FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D, false>,                                 \
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cells));         \
+        columns_kernel<D, true><<<(unsigned)blocks, kThreads, smem_count, c->stream>>>(cp);                    \
+        columns_scan<<<1, 1024, 0, c->stream>>>(cp.sums, (uint32_t)blocks, c->hdr);                            \
+        columns_kernel<D, false><<<(unsigned)blocks, kThreads, smem_cells, c->stream>>>(cp);                   \
+    } while (0)
+    switch (dialect) {
+    case FALX_CSV: FALX_COLS(D_CSV); break;
+    case FALX_CSV_HASH: FALX_COLS(D_CSV_HASH); break;
+    case FALX_TSV: FALX_COLS(D_TSV); break;
+    default: FALX_COLS(D_LOGFMT); break;
+    }
+#undef FALX_COLS
+    FALX_CUDA(cudaGetLastError());
+    FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->hhdr->error & (ERR_TIMEOUT | ERR_TMA)) return FALX_ERR_TIMEOUT;
+    for (int k = 0; k < kMaxStr; k++)
+        if (c->hhdr->arena[k] > 0x7FFFFFFFull) return FALX_ERR_OVERFLOW;  // i32 string offsets
+    return FALX_OK;
+}
+
 int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, uint64_t len, falx_outputs *o) {
     if (!schema || !o) return FALX_ERR_INVALID;
     int dialect = schema->dialect;
@@ -896,7 +842,8 @@ int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, ui
         if (o->stats) memset(o->stats, 0, sizeof *o->stats);
         return FALX_OK;
     }
-    rc = run_scan(c, dialect, rows, data, len, P);
+    if (rows && c->rows_path == 0) rc = rows_two_pass(c, dialect, data, len, P);
+    else rc = run_scan(c, dialect, rows, data, len, P);
     if (rc) return rc;
     const DevHeader &h = *c->hhdr;
     o->n_index = h.n_struct;
@@ -996,7 +943,26 @@ void falx_destroy(falx_ctx *c) {
     if (c->mlp_scratch) cudaFree(c->mlp_scratch);
     if (c->pred) cudaFree(c->pred);
     if (c->summary_dev) cudaFree(c->summary_dev);
+    if (c->tape_seps) cudaFree(c->tape_seps);
+    if (c->tape_ends) cudaFree(c->tape_ends);
+    if (c->rec_sums) cudaFree(c->rec_sums);
     delete c;
+}
+
+int falx_set_option(falx_ctx *c, int option, int value) {
+    if (!c) return FALX_ERR_INVALID;
+    switch (option) {
+    case FALX_OPT_ROWS_PATH:
+        if (value != 0 && value != 1) return FALX_ERR_INVALID;
+        c->rows_path = value;
+        return FALX_OK;
+    case FALX_OPT_CTAS_PER_SM:
+        if (value < 0) return FALX_ERR_INVALID;
+        c->ctas_per_sm = value;
+        return FALX_OK;
+    default:
+        return FALX_ERR_INVALID;
+    }
 }
 
 int falx_set_stream(falx_ctx *c, void *stream) {

@@ -138,19 +138,23 @@ __device__ __forceinline__ uint32_t cleaned_len(const uint8_t *s, uint32_t len) 
 }
 
 // Append the cleaned field to `dst` (csv_hash.rs:1749-1782); `cap` bounds it.
-__device__ __forceinline__ void copy_clean(const uint8_t *s, uint32_t len, uint8_t *dst, uint64_t at, uint64_t cap) {
+// Copies the cleaned bytes of a raw field to dst[at..] (bounded by cap)
+// and returns the cleaned length.
+__device__ __forceinline__ uint32_t copy_clean(const uint8_t *s, uint32_t len, uint8_t *dst, uint64_t at,
+                                               uint64_t cap) {
     if (len >= 2 && s[0] == '"' && s[len - 1] == '"') {
-        uint32_t il = len - 2, i = 0;
+        uint32_t il = len - 2, i = 0, o = 0;
         const uint8_t *in = s + 1;
         while (i < il) {
-            if (at < cap) dst[at] = in[i];
-            at++;
+            if (at + o < cap) dst[at + o] = in[i];
+            o++;
             i += (in[i] == '"' && i + 1 < il && in[i + 1] == '"') ? 2 : 1;
         }
-        return;
+        return o;
     }
-    for (uint32_t i = 0; i < len; i++, at++)
-        if (at < cap) dst[at] = s[i];
+    for (uint32_t i = 0; i < len; i++)
+        if (at + i < cap) dst[at + i] = s[i];
+    return len;
 }
 
 struct StatAcc {
@@ -435,20 +439,26 @@ __device__ void rows_fast(const RowSpec &rs, const RowCtx &rc, RowShared<true> &
         __syncthreads();
     }
 
-    // ---- numeric / bytes / validity: warps take 32 consecutive rows of one column
+    // ---- numeric / bytes / validity: warps take 32 consecutive rows of one
+    // column; with string columns warp 0 runs the arena look-back meanwhile
     const uint32_t rpad = (nrows + 31) & ~31u;
     const uint32_t ncell = rpad * (uint32_t)rs.ncols;
-    for (uint32_t i = tid; i < ncell; i += kThreads) {
+    const uint32_t w0 = rs.nstr > 0 ? 32u : 0u;
+    for (uint32_t i = (uint32_t)tid - w0; (uint32_t)tid >= w0 && i < ncell; i += kThreads - w0) {
         const int c = (int)(i / rpad);
         const uint32_t r = i % rpad;
         bool ok = false;
         if (r < nrows) {
             const uint64_t g = (uint64_t)rc.row_base + r;
             const Cell cl = cell_span(rc, sh, stage, n_total, n_term_all, r, rs.field[c]);
-            uint32_t dummy[kMaxStr] = {0, 0, 0, 0};
-            const uint32_t n = (uint32_t)(cl.to - cl.from);
-            ok = decode_cell(rs, c, g, cl.present ? cell_ptr(rc, cl.from, cl.to) : nullptr, n, cl.present, cl.from,
-                             cl.to, dummy);
+            if (rs.type[c] == 3) {
+                ok = cl.present;  // lengths and bytes are handled by the arena pass
+            } else {
+                uint32_t dummy[kMaxStr] = {0, 0, 0, 0};
+                const uint32_t n = (uint32_t)(cl.to - cl.from);
+                ok = decode_cell(rs, c, g, cl.present ? cell_ptr(rc, cl.from, cl.to) : nullptr, n, cl.present,
+                                 cl.from, cl.to, dummy);
+            }
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, ok);
         if (lane == 0 && bal) {
@@ -457,6 +467,16 @@ __device__ void rows_fast(const RowSpec &rs, const RowCtx &rc, RowShared<true> &
             atomicOr((unsigned long long *)&sh.vbits[c][w], (unsigned long long)bal << sh6);
             if (sh6 > 32) atomicOr((unsigned long long *)&sh.vbits[c][w + 1], (unsigned long long)bal >> (64 - sh6));
         }
+    }
+
+    // ---- string arenas: the tile's arena offsets (warp 0, overlapping the cells)
+    if (rs.nstr > 0 && warp == 0) {
+        uint32_t tot[kMaxStr];
+        for (int k = 0; k < kMaxStr; k++) tot[k] = sh.tile_len[k];
+        unsigned long long pre[kMaxStr];
+        arena_lookback(rc, tot, lane, pre);
+        if (lane == 0)
+            for (int k = 0; k < kMaxStr; k++) sh.arena_base[k] = (uint32_t)pre[k];
     }
 
     // ---- count / sum sink over two fields
@@ -500,15 +520,6 @@ __device__ void rows_fast(const RowSpec &rs, const RowCtx &rc, RowShared<true> &
         }
     }
 
-    // ---- string arenas: look-back for the tile's arena offsets, then copy
-    if (rs.nstr > 0 && warp == 0) {
-        uint32_t tot[kMaxStr];
-        for (int k = 0; k < kMaxStr; k++) tot[k] = sh.tile_len[k];
-        unsigned long long pre[kMaxStr];
-        arena_lookback(rc, tot, lane, pre);
-        if (lane == 0)
-            for (int k = 0; k < kMaxStr; k++) sh.arena_base[k] = (uint32_t)pre[k];
-    }
     __syncthreads();
 
     // validity words (row bits staged relative to the tile's first row)
@@ -537,8 +548,7 @@ __device__ void rows_fast(const RowSpec &rs, const RowCtx &rc, RowShared<true> &
                 if (cl.present) {
                     const uint32_t n = (uint32_t)(cl.to - cl.from);
                     const uint8_t *src = cell_ptr(rc, cl.from, cl.to);
-                    copy_clean(src, n, rs.str_data[c], at, rs.str_cap[c]);
-                    at += cleaned_len(src, n);
+                    at += copy_clean(src, n, rs.str_data[c], at, rs.str_cap[c]);
                 }
                 if (g < rs.rows_cap) static_cast<int32_t *>(rs.values[c])[g + 1] = (int32_t)at;
             }

@@ -84,6 +84,13 @@ struct Params {
 
 // Shared state of the block-wide look-back.
 
+// Shared state of the block-wide look-back.
+struct LookbackSmem {
+    uint32_t wf[kWarps];
+    unsigned long long wc[kWarps][4];
+    uint32_t first_incl[3], first_wait[3], stop, entry, pre[3], restart;
+};
+
 // Shared-memory layout (dynamic); NB tile buffers in flight.
 template <bool ROWS, int NB = 2>
 struct Smem {
@@ -99,6 +106,7 @@ struct Smem {
     uint32_t tile_f;
     uint32_t base[3];       // global structural / terminator / row offsets of the tile
     unsigned long long tile_c;
+    LookbackSmem lb;
     RowShared<ROWS> rs;
 };
 
@@ -167,32 +175,6 @@ template <int D>
 struct NStates {
     static constexpr int value = D == D_TSV ? 1 : D == D_CSV ? 2 : D == D_CSV_HASH ? 3 : 4;
 };
-
-// Warp-wide spin until every lane's status word (lane l watches tile
-// hi - l) reaches `level` in this launch's epoch. Returns each lane's flag,
-// or sets `gave_up` after the wait bound or an abort.
-__device__ __forceinline__ uint32_t window_wait(const Params &p, int64_t hi, int lane, uint32_t level,
-                                                bool &gave_up) {
-    const int64_t j = hi - lane;
-    const bool in = j >= 0;
-    const uint64_t t0 = globaltimer_ns();
-    uint32_t flag = 0;
-    for (uint32_t it = 0;; it++) {
-        if (in) flag = ld_acquire(&p.status[j].flag);
-        bool ready = !in || ((flag >> 2) == p.epoch && (flag & 3) >= level);
-        if (__all_sync(0xffffffffu, ready)) break;
-        if ((it & 63) == 63) {
-            bool stop = lane == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
-            if (__any_sync(0xffffffffu, stop)) {
-                if (lane == 0) fail(p.hdr, ERR_TIMEOUT);
-                gave_up = true;
-                return 0;
-            }
-        }
-        __nanosleep(32);
-    }
-    return flag;
-}
 
 __device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t *p) {
     uint64_t v;
@@ -274,93 +256,151 @@ __device__ __forceinline__ void agg_prepend_spec(uint32_t gf, const uint64_t (&g
     f = fcompose(gf, f);
 }
 
-// Decoupled look-back over (transfer function, counts per entry state)
-// aggregates, run by one warp: lane l watches predecessor hi - l. A probe
-// ends as soon as every predecessor nearer than the nearest published
-// inclusive prefix has published its aggregate (it never waits on older
-// tiles than it needs); without an inclusive prefix in the window it needs the
-// whole window and moves 32 tiles further back. Combining an older segment A
-// with a newer B gives (f_B . f_A, c_A[s] + c_B[f_A(s)]). Returns the tile's
-// entry state and the counts of the file before the tile.
-template <int NS>
-__device__ uint32_t lookback(const Params &p, uint32_t tile, int lane, uint32_t pre[3]) {
-    uint32_t af = kIdentity;  // aggregate of the tiles between the window and `tile`
+// Block-wide look-back (all threads): thread t watches predecessor
+// tile - 1 - t. Waits only for the predecessors nearer than the nearest
+// published inclusive prefix (level kIncl); returns the tile's entry state,
+// the counts of the file before it and, for speculative aggregates, whether
+// some of those counts are not known yet.
+//
+// Speculative status levels: 1 = the tile's full transfer function, the
+// entry state it assumed and its counts under that assumption; 2 = its true
+// exit state and its counts under its true entry (published by a tile whose
+// assumption was wrong, as soon as its look-back knows its entry); 3 = its
+// inclusive prefix. The entry state never waits on counts: it follows from
+// the transfer functions alone. A level-1 tile that assumed the wrong entry
+// makes the counts unknown until it reaches level 2.
+template <int NS, bool SPEC>
+__device__ void lookback_cta(const Params &p, LookbackSmem &L, uint32_t tile, uint32_t &entry, uint32_t pre[3],
+                             bool &unknown) {
+    constexpr uint32_t kIncl = SPEC ? 3 : 2;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t af = kIdentity;  // thread 0: aggregate between the window and `tile`
     uint32_t ac[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     uint32_t au = 0;
     const uint64_t t0 = globaltimer_ns();
-    for (int64_t hi = (int64_t)tile - 1; hi >= 0; hi -= 32) {
-        const int64_t j = hi - lane;
+    unknown = false;
+    if (tile == 0) {
+        entry = p.entry0;
+        pre[0] = pre[1] = pre[2] = 0;
+        return;
+    }
+    for (int64_t hi = (int64_t)tile - 1; hi >= 0; hi -= kThreads) {
+        const int64_t j = hi - tid;
         const bool in = j >= 0;
-        uint32_t flag = 0, ball_incl = 0;
+        uint32_t flag = 0;
+        uint32_t sidx;
+        // Three rotating slots for the block-wide minima: in poll iteration
+        // `it` thread 0 resets slot it+1 before the barrier, every thread
+        // updates slot it before it and reads slot it after it. No slot is
+        // reset while a thread may still read it.
+        if (tid == 0) {
+            L.first_incl[0] = L.first_wait[0] = kThreads;
+        }
+        __syncthreads();
         for (uint32_t it = 0;; it++) {
+            const uint32_t sl = it % 3, nx = (it + 1) % 3;
+            if (tid == 0) L.first_incl[nx] = L.first_wait[nx] = kThreads;
             if (in) flag = ld_acquire(&p.status[j].flag);
             const bool cur = (flag >> 2) == p.epoch;
-            const uint32_t not_ready = __ballot_sync(0xffffffffu, in && !(cur && (flag & 3) >= 1));
-            ball_incl = __ballot_sync(0xffffffffu, in && cur && (flag & 3) >= 2);
-            const int first_incl = ball_incl ? __ffs(ball_incl) - 1 : 32;
-            const int first_wait = not_ready ? __ffs(not_ready) - 1 : 32;
-            if (first_wait > first_incl || not_ready == 0) break;
-            if ((it & 63) == 63) {
-                const bool stop = lane == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
-                if (__any_sync(0xffffffffu, stop)) {
-                    if (lane == 0) fail(p.hdr, ERR_TIMEOUT);
+            const bool waitv = in && !(cur && (flag & 3) >= 1);
+            const bool incl = in && cur && (flag & 3) >= kIncl;
+            const uint32_t bw = __ballot_sync(0xffffffffu, waitv), bi = __ballot_sync(0xffffffffu, incl);
+            if (lane == 0 && bw) atomicMin(&L.first_wait[sl], (uint32_t)(warp * 32 + __ffs(bw) - 1));
+            if (lane == 0 && bi) atomicMin(&L.first_incl[sl], (uint32_t)(warp * 32 + __ffs(bi) - 1));
+            __syncthreads();
+            const uint32_t fw = L.first_wait[sl], fi = L.first_incl[sl];
+            sidx = fi;
+            if (fw > fi || fw == (uint32_t)kThreads) break;
+            if ((it & 15) == 15) {
+                const bool stop = tid == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
+                if (__syncthreads_or(stop)) {
+                    if (tid == 0) fail(p.hdr, ERR_TIMEOUT);
+                    entry = 0;
                     pre[0] = pre[1] = pre[2] = 0;
-                    return 0;
+                    return;
                 }
             }
-            __nanosleep(32);
+            __nanosleep(64);
         }
-        const int sidx = ball_incl ? __ffs(ball_incl) - 1 : 32;
         uint32_t f = kIdentity;
         uint64_t c[4] = {0, 0, 0, 0};
-        if (in && lane < sidx) {
-            f = ld_relaxed(&p.status[j].func);
+        if (in && (uint32_t)tid < sidx) {
+            if (!SPEC) {
+                f = ld_relaxed(&p.status[j].func);
 #pragma unroll
-            for (int s = 0; s < NS; s++) c[s] = ld_relaxed64(&p.status[j].agg[s]);
+                for (int s0 = 0; s0 < NS; s0++) c[s0] = ld_relaxed64(&p.status[j].agg[s0]);
+            } else if ((flag & 3) >= 2) {
+                f = fconst(ld_relaxed(&p.status[j].exit));
+                const uint64_t v = ld_relaxed64(&p.status[j].agg[1]);
+#pragma unroll
+                for (int s0 = 0; s0 < NS; s0++) c[s0] = v;
+            } else {
+                const uint32_t pf = ld_relaxed(&p.status[j].func);
+                f = pf & 0xFF;
+                if ((pf >> 8) == kAllStates) {
+#pragma unroll
+                    for (int s0 = 0; s0 < NS; s0++) c[s0] = ld_relaxed64(&p.status[j].agg[s0]);
+                } else {
+                    const uint64_t v = ld_relaxed64(&p.status[j].agg[0]);
+#pragma unroll
+                    for (int s0 = 0; s0 < NS; s0++) c[s0] = (uint32_t)s0 == (pf >> 8) ? v : kUnknown;
+                }
+            }
         }
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const uint32_t gf = __shfl_down_sync(0xffffffffu, f, d);
             uint64_t gc[4];
 #pragma unroll
-            for (int s = 0; s < NS; s++) gc[s] = __shfl_down_sync(0xffffffffu, c[s], d);
-            if (lane + d < 32) agg_prepend<NS>(gf, gc, f, c);  // lane + d covers older tiles
-        }
-        uint32_t wf = __shfl_sync(0xffffffffu, f, 0);
-        unsigned long long wc[4];
-#pragma unroll
-        for (int s = 0; s < NS; s++) wc[s] = __shfl_sync(0xffffffffu, c[s], 0);
-        wide_prepend<NS>(wf, wc, af, ac, au);
-        if (ball_incl) {
-            uint32_t ex = 0, i0 = 0, i1 = 0, i2 = 0;
-            if (lane == sidx) {
-                ex = ld_relaxed(&p.status[j].exit);
-                i0 = ld_relaxed(&p.status[j].incl[0]);
-                i1 = ld_relaxed(&p.status[j].incl[1]);
-                i2 = ld_relaxed(&p.status[j].incl[2]);
+            for (int s0 = 0; s0 < NS; s0++) gc[s0] = __shfl_down_sync(0xffffffffu, c[s0], d);
+            if (lane + d < 32) {
+                if (SPEC) agg_prepend_spec<NS>(gf, gc, f, c);
+                else agg_prepend<NS>(gf, gc, f, c);
             }
-            ex = __shfl_sync(0xffffffffu, ex, sidx);
-            uint32_t c0 = ac[0][0], c1 = ac[0][1], c2 = ac[0][2];
-#pragma unroll
-            for (int t = 1; t < NS; t++)
-                if (ex == (uint32_t)t) { c0 = ac[t][0]; c1 = ac[t][1]; c2 = ac[t][2]; }
-            pre[0] = __shfl_sync(0xffffffffu, i0, sidx) + c0;
-            pre[1] = __shfl_sync(0xffffffffu, i1, sidx) + c1;
-            pre[2] = __shfl_sync(0xffffffffu, i2, sidx) + c2;
-            return fapply(af, ex);
         }
-    }
-    // reached the first tile: a file starts outside every region, a shard
-    // in its seed state
-    const uint32_t e0 = p.entry0;
-    uint32_t c0 = ac[0][0], c1 = ac[0][1], c2 = ac[0][2];
+        if (lane == 0) {
+            L.wf[warp] = f;
 #pragma unroll
-    for (int t = 1; t < NS; t++)
-        if (e0 == (uint32_t)t) { c0 = ac[t][0]; c1 = ac[t][1]; c2 = ac[t][2]; }
-    pre[0] = c0;
-    pre[1] = c1;
-    pre[2] = c2;
-    return fapply(af, e0);
+            for (int s0 = 0; s0 < NS; s0++) L.wc[warp][s0] = c[s0];
+        }
+        if ((uint32_t)tid == sidx) {
+            L.entry = ld_relaxed(&p.status[j].exit);
+            L.pre[0] = ld_relaxed(&p.status[j].incl[0]);
+            L.pre[1] = ld_relaxed(&p.status[j].incl[1]);
+            L.pre[2] = ld_relaxed(&p.status[j].incl[2]);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 0; w < kWarps; w++) {
+                unsigned long long g[4];
+#pragma unroll
+                for (int s0 = 0; s0 < NS; s0++) g[s0] = L.wc[w][s0];
+                wide_prepend<NS>(L.wf[w], g, af, ac, au);
+            }
+            const bool found = sidx < (uint32_t)kThreads;
+            const bool at_start = hi - kThreads < 0;
+            L.stop = found || at_start;
+            if (found || at_start) {
+                const uint32_t ex = found ? L.entry : p.entry0;
+                uint32_t c0 = ac[0][0], c1 = ac[0][1], c2 = ac[0][2];
+#pragma unroll
+                for (int t = 1; t < NS; t++)
+                    if (ex == (uint32_t)t) { c0 = ac[t][0]; c1 = ac[t][1]; c2 = ac[t][2]; }
+                L.pre[0] = (found ? L.pre[0] : 0u) + c0;
+                L.pre[1] = (found ? L.pre[1] : 0u) + c1;
+                L.pre[2] = (found ? L.pre[2] : 0u) + c2;
+                L.entry = fapply(af, ex);
+                L.restart = (au >> ex) & 1u;
+            }
+        }
+        __syncthreads();
+        if (L.stop) break;
+    }
+    entry = L.entry;
+    pre[0] = L.pre[0];
+    pre[1] = L.pre[1];
+    pre[2] = L.pre[2];
+    unknown = SPEC && L.restart;
 }
 
 // The byte before position 0 of a launch: -1 at the start of a file.
@@ -480,10 +520,11 @@ __device__ __forceinline__ void process_tile(const Params &p, Smem<ROWS, NB> &S,
         for (int s0 = 0; s0 < NS; s0++) tst->agg[s0] = agg[s0];
         st_release(&tst->flag, p.epoch * 4 + 1);
     }
-    if (warp == 0) {
-        uint32_t pre[3];
-        const uint32_t e = lookback<NS>(p, tile, lane, pre);
-        if (lane == 0) {
+    {
+        uint32_t pre[3], e;
+        bool unknown;
+        lookback_cta<NS, false>(p, S.lb, tile, e, pre, unknown);
+        if (tid == 0) {
             unsigned long long mine = agg[0];
 #pragma unroll
             for (int t = 1; t < NS; t++) mine = e == (uint32_t)t ? agg[t] : mine;

@@ -60,6 +60,13 @@ typedef struct falx_ctx falx_ctx;
 /* Context: device, stream, look-back scratch, tuned launch parameters. */
 int falx_create(int device, falx_ctx **out);
 void falx_destroy(falx_ctx *ctx);
+/* Options. FALX_OPT_ROWS_PATH: how rows (columns, field bytes, count/sum)
+ * are made: 0 (default) index + tape pass, then a record-parallel pass over
+ * the tape; 1 one fused tile pass. Same outputs either way.
+ * FALX_OPT_CTAS_PER_SM caps the persistent grids (0 = as many as fit). */
+#define FALX_OPT_ROWS_PATH 1
+#define FALX_OPT_CTAS_PER_SM 2
+int falx_set_option(falx_ctx *ctx, int option, int value);
 /* Use `stream` (a cudaStream_t; NULL = the legacy default stream). */
 int falx_set_stream(falx_ctx *ctx, void *stream);
 const char *falx_strerror(int code);
