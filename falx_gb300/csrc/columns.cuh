@@ -72,6 +72,16 @@ struct ColSmem {
     alignas(16) uint8_t data[kDataWin];  // last: the count pass launches without it
 };
 
+// Asynchronous global -> shared copies (all of a CTA's copies in flight at
+// once; completed by cp_async_wait_all + a barrier).
+template <int N>
+__device__ __forceinline__ void cp_async_ca(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "n"(N)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 struct Rec {
     int64_t start, end;  // [start, end): the record without its terminator
     uint64_t sb;         // index of its first separator in `seps`
@@ -104,6 +114,77 @@ struct ColView {
     }
 };
 
+// Common cell shapes, decoded inline; anything else goes to the general
+// decoders (kept out of line so the per-cell loop stays small). A fast path
+// that accepts a cell gives exactly the general decoder's value.
+
+// 1-9 plain digits.
+__device__ __forceinline__ bool fast_u32(const uint8_t *s, uint32_t n, uint32_t &v) {
+    if (n == 0 || n > 9) return false;
+    uint32_t x = 0;
+    for (uint32_t k = 0; k < n; k++) {
+        const uint32_t d = (uint32_t)s[k] - '0';
+        if (d > 9) return false;
+        x = x * 10 + d;
+    }
+    v = x;
+    return true;
+}
+
+// [+-]?d{1,3}.d{6}: m / 1e6 correctly rounded (csv_geo.rs:1414-1475).
+__device__ __forceinline__ bool fast_fixed6(const uint8_t *s, uint32_t n, uint64_t &bits) {
+    if (n < 8 || n > 11) return false;
+    const uint8_t c0 = s[0];
+    const uint32_t i = (c0 == '-' || c0 == '+') ? 1u : 0u;
+    if (n - i < 8 || n - i > 10 || s[n - 7] != '.') return false;
+    uint32_t frac = 0, ip = 0;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const uint32_t d = (uint32_t)s[n - 6 + k] - '0';
+        if (d > 9) return false;
+        frac = frac * 10 + d;
+    }
+    for (uint32_t k = i; k + 7 < n; k++) {
+        const uint32_t d = (uint32_t)s[k] - '0';
+        if (d > 9) return false;
+        ip = ip * 10 + d;
+    }
+    bits = dec::eisel_lemire((uint64_t)ip * 1000000u + frac, -6) | ((uint64_t)(c0 == '-') << 63);
+    return true;
+}
+
+__device__ __noinline__ bool slow_i64(const uint8_t *s, uint32_t n, int64_t &v) {
+    return dec::numeric_view(s, n) && dec::parse_i64(s, n, v);
+}
+__device__ __noinline__ bool slow_u32(const uint8_t *s, uint32_t n, uint32_t &v) {
+    return dec::numeric_view(s, n) && dec::parse_u32(s, n, v);
+}
+__device__ __noinline__ bool slow_f64(const uint8_t *s, uint32_t n, uint64_t &bits) {
+    double v;
+    if (!(dec::numeric_view(s, n) && dec::parse_f64(s, n, v))) return false;
+    bits = dec::d2u(v);
+    return true;
+}
+
+// Count / sum of one f64 cell (csv_geo.rs:1735-1750): values, bit checksum,
+// exact x1e6 sum. The fixed shape needs no general decoder.
+__device__ __noinline__ void stat_slow(StatAcc &a, int k, const uint8_t *s, uint32_t n) { stat_cell(a, k, s, n); }
+__device__ __forceinline__ void stat_value(StatAcc &a, int k, const uint8_t *s, uint32_t n) {
+    uint64_t bits;
+    if (fast_fixed6(s, n, bits)) {
+        // d{1,3}.d{6} is exact in micro-units: +-(ip * 1e6 + frac)
+        const uint32_t i = (s[0] == '-' || s[0] == '+') ? 1u : 0u;
+        int64_t e6 = 0;
+        for (uint32_t q = i; q < n; q++)
+            if (s[q] != '.') e6 = e6 * 10 + (s[q] - '0');
+        a.values[k]++;
+        a.checksum[k] += bits;
+        a.sum_e6[k] += (unsigned long long)(s[0] == '-' ? -e6 : e6);
+        return;
+    }
+    stat_slow(a, k, s, n);
+}
+
 // A non-string cell (I64, U32, F64, BYTES) of row g: stores the value (a
 // zero placeholder when invalid) and returns its validity.
 __device__ __forceinline__ bool decode_value(const RowSpec &rs, int c, uint64_t g, const uint8_t *s, uint32_t n,
@@ -113,28 +194,16 @@ __device__ __forceinline__ bool decode_value(const RowSpec &rs, int c, uint64_t 
     bool ok = false;
     if (ty == 0) {
         int64_t v = 0;
-        if (present) {
-            const uint8_t *q = s;
-            uint32_t l = n;
-            ok = dec::numeric_view(q, l) && dec::parse_i64(q, l, v);
-        }
+        if (present) ok = slow_i64(s, n, v);
         if (store) static_cast<int64_t *>(rs.values[c])[g] = ok ? v : 0;
     } else if (ty == 1) {
         uint32_t v = 0;
-        if (present) {
-            const uint8_t *q = s;
-            uint32_t l = n;
-            ok = dec::numeric_view(q, l) && dec::parse_u32(q, l, v);
-        }
+        if (present) ok = fast_u32(s, n, v) || slow_u32(s, n, v);
         if (store) static_cast<uint32_t *>(rs.values[c])[g] = ok ? v : 0u;
     } else if (ty == 2) {
-        double v = 0.0;
-        if (present) {
-            const uint8_t *q = s;
-            uint32_t l = n;
-            ok = dec::numeric_view(q, l) && dec::parse_f64(q, l, v);
-        }
-        if (store) static_cast<double *>(rs.values[c])[g] = ok ? v : 0.0;
+        uint64_t bits = 0;
+        if (present) ok = fast_fixed6(s, n, bits) || slow_f64(s, n, bits);
+        if (store) static_cast<uint64_t *>(rs.values[c])[g] = ok ? bits : 0ull;
     } else {
         ok = present && n > 0;
         if (store) {
@@ -160,8 +229,9 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
     // ---- stage the tape entries of the block's records
     for (int i = tid; i <= kRecBlock; i += kThreads) {
         const int64_t e = (int64_t)R0 - 1 + i;
-        if (e >= 0 && (uint64_t)e < p.n_ends) S.ends[i] = p.ends[e];
+        if (e >= 0 && (uint64_t)e < p.n_ends) cp_async_ca<8>(&S.ends[i], p.ends + e);
     }
+    cp_async_wait_all();
     __syncthreads();
     if (tid == 0) {
         // separator and byte windows: from the block's first record to its last
@@ -182,12 +252,12 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
         S.data_n = COUNT ? 0u : (uint32_t)qn;
     }
     __syncthreads();
-    for (uint32_t i = tid; i < S.sep_n; i += kThreads) S.seps[i] = p.seps[S.sep_lo + i];
+    for (uint32_t i = tid; i < S.sep_n; i += kThreads) cp_async_ca<4>(&S.seps[i], p.seps + S.sep_lo + i);
     if (!COUNT) {
-        const uint4 *src = reinterpret_cast<const uint4 *>(p.abase + (S.data_lo + p.shift));
-        uint4 *dst = reinterpret_cast<uint4 *>(S.data);
-        for (uint32_t i = tid; i < S.data_n / 16; i += kThreads) dst[i] = src[i];
+        const uint8_t *src = p.abase + (S.data_lo + p.shift);
+        for (uint32_t i = tid; i < S.data_n / 16; i += kThreads) cp_async_ca<16>(S.data + 16 * i, src + 16 * i);
     }
+    cp_async_wait_all();
     __syncthreads();
     const ColView V{p, S};
 
@@ -318,7 +388,7 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
             acc.records++;
             for (int k = 0; k < 2; k++) {
                 int64_t a, b;
-                if (V.field(x, rs.stats_field[k], a, b)) stat_cell(acc, k, V.bytes(a, b), (uint32_t)(b - a));
+                if (V.field(x, rs.stats_field[k], a, b)) stat_value(acc, k, V.bytes(a, b), (uint32_t)(b - a));
             }
         }
         if (rs.want_fb) {
@@ -396,29 +466,26 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
 
 namespace falx {
 
-// Exclusive prefixes of the per-block sums (one CTA of 1024 threads, each
-// a run of consecutive blocks), and the totals.
+// Exclusive prefixes of the per-block sums, and the totals. One CTA of
+// 1024 threads; warp w owns a contiguous run of blocks and reads it 32
+// entries at a time (coalesced): first its total, then, after a scan of the
+// 32 totals, the prefixes.
 __global__ void __launch_bounds__(1024) columns_scan(RecSums *sums, uint32_t n, DevHeader *hdr) {
     __shared__ unsigned long long wsum[32][1 + kMaxStr];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const uint32_t per = (n + 1023) / 1024, lo = min(n, t * per), hi = min(n, lo + per);
-    unsigned long long run[1 + kMaxStr] = {0, 0, 0, 0, 0};
-    for (uint32_t i = lo; i < hi; i++) {
+    const uint32_t per = (n + 31) / 32, lo = min(n, warp * per), hi = min(n, lo + per);
+    unsigned long long tot[1 + kMaxStr] = {0, 0, 0, 0, 0};
+    for (uint32_t i = lo + lane; i < hi; i += 32) {
         const RecSums v = sums[i];
-        run[0] += v.rows;
-        for (int k = 0; k < kMaxStr; k++) run[1 + k] += v.arena[k];
+        tot[0] += v.rows;
+#pragma unroll
+        for (int k = 0; k < kMaxStr; k++) tot[1 + k] += v.arena[k];
     }
-    unsigned long long ex[1 + kMaxStr];
 #pragma unroll
     for (int k = 0; k < 1 + kMaxStr; k++) {
-        unsigned long long x = run[k];
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const unsigned long long o = __shfl_up_sync(0xffffffffu, x, d);
-            if (lane >= d) x += o;
-        }
-        ex[k] = x - run[k];
-        if (lane == 31) wsum[warp][k] = x;
+        for (int d = 16; d > 0; d >>= 1) tot[k] += __shfl_xor_sync(0xffffffffu, tot[k], d);
+        if (lane == 0) wsum[warp][k] = tot[k];
     }
     __syncthreads();
     if (warp == 0) {
@@ -439,16 +506,28 @@ __global__ void __launch_bounds__(1024) columns_scan(RecSums *sums, uint32_t n, 
         }
     }
     __syncthreads();
-    unsigned long long pre[1 + kMaxStr];
+    unsigned long long carry[1 + kMaxStr];
 #pragma unroll
-    for (int k = 0; k < 1 + kMaxStr; k++) pre[k] = wsum[warp][k] + ex[k];
-    for (uint32_t i = lo; i < hi; i++) {
-        const RecSums v = sums[i];
-        sums[i].rows = (uint32_t)pre[0];
-        pre[0] += v.rows;
-        for (int k = 0; k < kMaxStr; k++) {
-            sums[i].arena[k] = (uint32_t)pre[1 + k];
-            pre[1 + k] += v.arena[k];
+    for (int k = 0; k < 1 + kMaxStr; k++) carry[k] = wsum[warp][k];
+    for (uint32_t i0 = lo; i0 < hi; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        RecSums v = {};
+        if (i < hi) v = sums[i];
+        uint32_t val[1 + kMaxStr] = {v.rows, v.arena[0], v.arena[1], v.arena[2], v.arena[3]};
+#pragma unroll
+        for (int k = 0; k < 1 + kMaxStr; k++) {
+            unsigned long long x = val[k];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned long long o = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= d) x += o;
+            }
+            const unsigned long long ex = carry[k] + x - val[k];
+            carry[k] += __shfl_sync(0xffffffffu, x, 31);
+            if (i < hi) {
+                if (k == 0) sums[i].rows = (uint32_t)ex;
+                else sums[i].arena[k - 1] = (uint32_t)ex;
+            }
         }
     }
 }
