@@ -185,6 +185,23 @@ __device__ __forceinline__ void stat_value(StatAcc &a, int k, const uint8_t *s, 
     stat_slow(a, k, s, n);
 }
 
+// A string cell's cleaned bytes into the arena at `at` (bounded by cap);
+// returns the cleaned length. Unquoted cells are copied with byte stores up
+// to a 4-byte boundary of the destination and word stores after it.
+__device__ __forceinline__ uint32_t copy_cell(const uint8_t *s, uint32_t n, uint8_t *arena, uint64_t at,
+                                              uint64_t cap) {
+    if ((n >= 2 && s[0] == '"' && s[n - 1] == '"') || at + n > cap) return copy_clean(s, n, arena, at, cap);
+    uint8_t *dst = arena + at;
+    uint32_t i = 0;
+    const uint32_t head = (uint32_t)((4 - ((uintptr_t)dst & 3)) & 3);
+    for (; i < head && i < n; i++) dst[i] = s[i];
+    for (; i + 4 <= n; i += 4)
+        *reinterpret_cast<uint32_t *>(dst + i) = (uint32_t)s[i] | ((uint32_t)s[i + 1] << 8) |
+                                                 ((uint32_t)s[i + 2] << 16) | ((uint32_t)s[i + 3] << 24);
+    for (; i < n; i++) dst[i] = s[i];
+    return n;
+}
+
 // A non-string cell (I64, U32, F64, BYTES) of row g: stores the value (a
 // zero placeholder when invalid) and returns its validity.
 __device__ __forceinline__ bool decode_value(const RowSpec &rs, int c, uint64_t g, const uint8_t *s, uint32_t n,
@@ -249,7 +266,7 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
         if (qn > kDataWin) qn = kDataWin;
         if (qn < 0) qn = 0;
         S.data_lo = q0 - p.shift;
-        S.data_n = COUNT ? 0u : (uint32_t)qn;
+        S.data_n = COUNT ? 0u : (uint32_t)qn;  // the count pass reads its few bytes in place
     }
     __syncthreads();
     for (uint32_t i = tid; i < S.sep_n; i += kThreads) cp_async_ca<4>(&S.seps[i], p.seps + S.sep_lo + i);
@@ -377,7 +394,7 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
             if (rs.type[c] == 3) {
                 const int k = rs.str_slot[c];
                 ok = present;
-                if (present) at[k] += copy_clean(V.bytes(a, b), n, rs.str_data[c], at[k], rs.str_cap[c]);
+                if (present) at[k] += copy_cell(V.bytes(a, b), n, rs.str_data[c], at[k], rs.str_cap[c]);
                 if (g < rs.rows_cap) static_cast<int32_t *>(rs.values[c])[g + 1] = (int32_t)at[k];
             } else {
                 ok = decode_value(rs, c, g, present ? V.bytes(a, b) : nullptr, n, present, a, b);

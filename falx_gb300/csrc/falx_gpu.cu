@@ -357,7 +357,9 @@ __global__ void __launch_bounds__(kThreads) index_kernel(const __grid_constant__
         LocalState cur;
         if (has_cur) {
             const bool ok = mbar_wait(&S.bar[s], phase[s], kWaitNs);
-            if (__syncthreads_or(!ok || (tid == 0 && aborted(p.hdr)))) {
+            // the abort flag (set by a CTA whose wait gave up) is read every
+            // 16th tile: every wait is bounded, so a late exit only costs time
+            if (__syncthreads_or(!ok || (tid == 0 && (i & 15) == 15 && aborted(p.hdr)))) {
                 if (tid == 0) {
                     if (!ok) fail(p.hdr, ERR_TMA);
                     else if (tile + G < p.num_tiles) mbar_wait(&S.bar[s ^ 1], phase[s ^ 1], kWaitNs);
@@ -769,6 +771,8 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     do {                                                                                                       \
         FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D, false>,                                 \
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cells));         \
+        FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D, true>,                                  \
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_count));         \
         columns_kernel<D, true><<<(unsigned)blocks, kThreads, smem_count, c->stream>>>(cp);                    \
         columns_scan<<<1, 1024, 0, c->stream>>>(cp.sums, (uint32_t)blocks, c->hdr);                            \
         columns_kernel<D, false><<<(unsigned)blocks, kThreads, smem_cells, c->stream>>>(cp);                   \
