@@ -83,14 +83,21 @@ class Clocks:
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons}
 
 
+STEP_KERNELS = ["index_kernel (index + tape)", "columns_kernel (count)", "columns_scan", "columns_kernel (cells)"]
+
+
 def measured_traffic(n):
-    """DRAM bytes per launch scaled from the committed ncu capture."""
+    """DRAM bytes of one step, per kernel and in total, scaled to n input
+    bytes from the committed ncu capture (the traffic of every kernel grows
+    in proportion to the input)."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            t = json.load(f)["scan_kernel<1, 1>"]
-        return int((t["dram_read"] + t["dram_write"]) * n / t["input_bytes"])
+            t = json.load(f)["csv_hash_parse_step"]
+        scale = n / t["input_bytes"]
+        per = {k: int((v["dram_read"] + v["dram_write"]) * scale) for k, v in t["kernels"].items()}
+        return sum(per.values()), per
     except Exception:
-        return None
+        return None, {}
 
 
 def make_input(size):
@@ -191,6 +198,9 @@ def bench_gpu(args):
     cs = schema.to_c()
     stream = torch.cuda.current_stream()
     eng.lib.falx_set_stream(eng.ctx, ctypes.c_void_p(stream.cuda_stream))
+    eng.lib.falx_set_option(eng.ctx, _lib.OPT_TIMING, 1)  # CUDA events around each launch of a step
+    kms = (ctypes.c_float * 4)()
+    kernel_ms = [[] for _ in STEP_KERNELS]
 
     # Size outputs from a first pass.
     idx_cap = n // 4 + 1024
@@ -230,6 +240,9 @@ def bench_gpu(args):
             ev1.record(stream)
             ev1.synchronize()
             per.append(ev0.elapsed_time(ev1))
+            if eng.lib.falx_last_timings(eng.ctx, kms, 4) == 4:
+                for k in range(4):
+                    kernel_ms[k].append(kms[k])
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     if dist:
@@ -246,6 +259,17 @@ def bench_gpu(args):
     algo = n + 4 * n_struct + rows * (4 + 4 + 8 + 8) + 5 * words * 8 + 4 * (rows + 1) + str_len
     peak, peak_kind = peaks()
     achieved = algo / (ms / 1e3) / 1e9
+    traffic, traffic_per = measured_traffic(n)
+    kernels = []
+    for name, ts in zip(STEP_KERNELS, kernel_ms):
+        if not ts:
+            continue
+        kt = sum(ts) / len(ts)
+        ent = {"name": name, "ms": round(kt, 4), "share": round(kt / ms, 4)}
+        if name in traffic_per:
+            ent["dram_bytes"] = traffic_per[name]
+            ent["dram_gbs"] = round(traffic_per[name] / (kt / 1e3) / 1e9, 1)
+        kernels.append(ent)
 
     # End to end through the host-buffer C ABI entry point.
     h_index = np.empty(idx_cap, dtype=np.uint32)
@@ -308,11 +332,14 @@ def bench_gpu(args):
                    "bytes": n, "structurals": int(n_struct), "rows": int(rows), "tile_bytes": 16384,
                    "l2": "input 1 GiB > L2, no flush", "parallelism": "replicas" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": measured_traffic(n), "peak_kind": peak_kind,
-                     "algorithmic_bytes": int(algo)},
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes": int(algo),
+                     "scope": "the whole step (index + tape pass, count, scan, cells): algorithmic bytes of the "
+                              "path / step time; traffic = DRAM bytes of the step's kernels"},
+        "kernels": kernels,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * len(STEP_KERNELS),
         "clocks": clk.summary(),
         "field_bytes": {"fields": fb.fields, "bytes": fb.bytes},
         "learned_speculation": spec,

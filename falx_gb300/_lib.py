@@ -87,6 +87,7 @@ SIGNATURES = {
     "falx_destroy": (None, [c_void_p]),
     "falx_set_stream": (c_int, [c_void_p, c_void_p]),
     "falx_set_option": (c_int, [c_void_p, c_int, c_int]),
+    "falx_last_timings": (c_int, [c_void_p, POINTER(c_float), c_int]),
     "falx_strerror": (c_char_p, [c_int]),
     "falx_index_structurals": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64)]),
     "falx_parse_tape": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, c_void_p, c_uint64,
@@ -136,6 +137,7 @@ SIGNATURES = {
 
 OPT_ROWS_PATH = 1
 OPT_CTAS_PER_SM = 2
+OPT_TIMING = 3
 MLP_BYTES = 256
 SPEC_TILE = 16384
 

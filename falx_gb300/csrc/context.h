@@ -56,4 +56,9 @@ struct falx_ctx {
     uint64_t tape_ends_cap = 0;     // bytes
     void *rec_sums = nullptr;
     uint64_t rec_sums_cap = 0;      // bytes
+    // per-launch timing of the last rows call (FALX_OPT_TIMING)
+    int timing = 0;
+    cudaEvent_t ev[5] = {};
+    float last_ms[4] = {};
+    int last_n = 0;
 };

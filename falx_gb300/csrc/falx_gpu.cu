@@ -731,6 +731,8 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     }
     const RowSpec rs = P.rows;
     memset(&P.rows, 0, sizeof P.rows);
+    c->last_n = 0;
+    if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[0], c->stream));
     int rc = run_scan(c, dialect, false, data, len, P);
     if (rc) return rc;
     uint64_t n_struct = c->hhdr->n_struct, n_terms = c->hhdr->n_terms;
@@ -748,6 +750,7 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
         rc = run_scan(c, dialect, false, data, len, P);
         if (rc) return rc;
     }
+    if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[1], c->stream));
     ColParams cp;
     memset(&cp, 0, sizeof cp);
     cp.data = data;
@@ -774,8 +777,11 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
         FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D, true>,                                  \
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_count));         \
         columns_kernel<D, true><<<(unsigned)blocks, kThreads, smem_count, c->stream>>>(cp);                    \
+        if (c->timing) cudaEventRecord(c->ev[2], c->stream);                                                   \
         columns_scan<<<1, 1024, 0, c->stream>>>(cp.sums, (uint32_t)blocks, c->hdr);                            \
+        if (c->timing) cudaEventRecord(c->ev[3], c->stream);                                                   \
         columns_kernel<D, false><<<(unsigned)blocks, kThreads, smem_cells, c->stream>>>(cp);                   \
+        if (c->timing) cudaEventRecord(c->ev[4], c->stream);                                                   \
     } while (0)
     switch (dialect) {
     case FALX_CSV: FALX_COLS(D_CSV); break;
@@ -787,6 +793,10 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     FALX_CUDA(cudaGetLastError());
     FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
     FALX_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->timing) {
+        for (int k = 0; k < 4; k++) cudaEventElapsedTime(&c->last_ms[k], c->ev[k], c->ev[k + 1]);
+        c->last_n = 4;
+    }
     if (c->hhdr->error & (ERR_TIMEOUT | ERR_TMA)) return FALX_ERR_TIMEOUT;
     for (int k = 0; k < kMaxStr; k++)
         if (c->hhdr->arena[k] > 0x7FFFFFFFull) return FALX_ERR_OVERFLOW;  // i32 string offsets
@@ -950,6 +960,8 @@ void falx_destroy(falx_ctx *c) {
     if (c->tape_seps) cudaFree(c->tape_seps);
     if (c->tape_ends) cudaFree(c->tape_ends);
     if (c->rec_sums) cudaFree(c->rec_sums);
+    for (int k = 0; k < 5; k++)
+        if (c->ev[k]) cudaEventDestroy(c->ev[k]);
     delete c;
 }
 
@@ -964,9 +976,20 @@ int falx_set_option(falx_ctx *c, int option, int value) {
         if (value < 0) return FALX_ERR_INVALID;
         c->ctas_per_sm = value;
         return FALX_OK;
+    case FALX_OPT_TIMING:
+        if (value && !c->ev[0])
+            for (int k = 0; k < 5; k++) FALX_CUDA(cudaEventCreate(&c->ev[k]));
+        c->timing = value != 0;
+        return FALX_OK;
     default:
         return FALX_ERR_INVALID;
     }
+}
+
+int falx_last_timings(const falx_ctx *c, float *ms, int n) {
+    if (!c || (n && !ms)) return FALX_ERR_INVALID;
+    for (int k = 0; k < n && k < c->last_n; k++) ms[k] = c->last_ms[k];
+    return c->last_n;
 }
 
 int falx_set_stream(falx_ctx *c, void *stream) {
