@@ -69,7 +69,8 @@ struct ColSmem {
     uint32_t data_n;
     uint64_t vbits[kMaxCols][kRecWords];
     unsigned long long red[kWarps][12];
-    alignas(16) uint8_t data[kDataWin];  // last: the count pass launches without it
+    alignas(16) uint8_t data[kDataWin + 16];  // last: the count pass launches without it; 16 bytes of
+                                              // slack for word reads that start near the window end
 };
 
 // Asynchronous global -> shared copies (all of a CTA's copies in flight at
@@ -82,158 +83,222 @@ __device__ __forceinline__ void cp_async_ca(void *dst, const void *src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// File positions and separator ordinals fit 32 bits (inputs are shorter
+// than 4 GiB), so the per-cell arithmetic is 32-bit.
 struct Rec {
-    int64_t start, end;  // [start, end): the record without its terminator
-    uint64_t sb;         // index of its first separator in `seps`
-    uint32_t nf;         // fields
-    bool row;            // a row (inside the file and not a comment)
+    uint32_t start, end;  // [start, end): the record without its terminator
+    uint32_t end2;        // end of its last field: `end` less a trailing '\r' (csv_geo.rs:1055-1060)
+    uint32_t sb;          // index of its first separator in `seps`
+    uint32_t nf;          // fields
+    bool row;             // a row (inside the file and not a comment)
 };
 
-struct ColView {
-    const ColParams &p;
-    const ColSmem &S;
-    __device__ __forceinline__ uint32_t sep(uint64_t i) const {
-        const uint64_t j = i - S.sep_lo;
-        return j < S.sep_n ? S.seps[j] : p.seps[i];
+// The block's staged windows with their bounds in registers (the cells
+// loop stores through generic pointers, after which shared-memory fields
+// would be read again).
+struct Win {
+    const uint32_t *sseps;
+    const uint8_t *sdata;
+    const uint32_t *gseps;
+    const uint8_t *gdata;
+    uint32_t sep_lo, sep_n;
+    uint32_t dlo, dn;  // staged bytes: file positions [dlo, dlo + dn), dlo taken mod 2^32
+    __device__ __forceinline__ uint32_t sep(uint32_t i) const {
+        const uint32_t j = i - sep_lo;
+        return j < sep_n ? sseps[j] : gseps[i];
     }
-    __device__ __forceinline__ const uint8_t *bytes(int64_t a, int64_t b) const {
-        return (a >= S.data_lo && b <= S.data_lo + (int64_t)S.data_n) ? S.data + (a - S.data_lo) : p.data + a;
+    // [a, a + n) is staged, at offset o (a before the window wraps to an
+    // offset above dn)
+    __device__ __forceinline__ bool staged(uint32_t a, uint32_t n, uint32_t &o) const {
+        o = a - dlo;
+        return o <= dn && n <= dn - o;
     }
-    // Field f of a record: [from, to), the last field without a '\r' before
-    // the record end (csv_geo.rs:1055-1060).
-    __device__ __forceinline__ bool field(const Rec &r, uint32_t f, int64_t &from, int64_t &to) const {
+    __device__ __forceinline__ const uint8_t *ptr(uint32_t a, uint32_t n) const {
+        uint32_t o;
+        return staged(a, n, o) ? sdata + o : gdata + a;
+    }
+    __device__ __forceinline__ uint8_t byte(uint32_t a) const { return *ptr(a, 1); }
+    // field f of record r: [from, to)
+    __device__ __forceinline__ bool field(const Rec &r, uint32_t f, uint32_t &from, uint32_t &to) const {
         if (f >= r.nf) return false;
-        from = f == 0 ? r.start : (int64_t)sep(r.sb + f - 1) + 1;
-        if (f + 1 < r.nf) {
-            to = (int64_t)sep(r.sb + f);
-        } else {
-            to = r.end;
-            if (to > r.start && bytes(to - 1, to)[0] == '\r') to--;
-        }
+        from = f == 0 ? r.start : sep(r.sb + f - 1) + 1;
+        to = f + 1 < r.nf ? sep(r.sb + f) : r.end2;
         return true;
     }
 };
 
-// Common cell shapes, decoded inline; anything else goes to the general
-// decoders (kept out of line so the per-cell loop stays small). A fast path
-// that accepts a cell gives exactly the general decoder's value.
+// ---- word-at-a-time (SWAR) cell decoding from the staged bytes.
+// Shared-memory words at any byte offset: two aligned loads and a funnel
+// shift per 32-bit word (little-endian: the first byte is the low byte).
+__device__ __forceinline__ uint32_t lds_u32(const uint8_t *base, uint32_t o) {
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(base + (o & ~3u));
+    return __funnelshift_r(w[0], w[1], 8u * (o & 3u));
+}
+__device__ __forceinline__ uint64_t lds_u64(const uint8_t *base, uint32_t o) {
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(base + (o & ~3u));
+    const uint32_t sh = 8u * (o & 3u), a = w[0], b = w[1], c = w[2];
+    return (uint64_t)__funnelshift_r(a, b, sh) | ((uint64_t)__funnelshift_r(b, c, sh) << 32);
+}
 
-// 1-9 plain digits.
-__device__ __forceinline__ bool fast_u32(const uint8_t *s, uint32_t n, uint32_t &v) {
-    if (n == 0 || n > 9) return false;
-    uint32_t x = 0;
-    for (uint32_t k = 0; k < n; k++) {
-        const uint32_t d = (uint32_t)s[k] - '0';
-        if (d > 9) return false;
-        x = x * 10 + d;
-    }
-    v = x;
+// Every byte of x that `keep` selects (0xFF per byte) is an ASCII digit.
+// Per byte b < 0x80: b + 0x46 reaches bit 7 iff b > '9'; (b | 0x80) - 0x30
+// keeps bit 7 iff b >= '0' and never borrows. Only a byte >= 0xBA carries
+// into the byte above it; such a byte fails the test itself when kept, and
+// the callers' unkept bytes are zero, or a digit and '.' checked elsewhere.
+__device__ __forceinline__ bool digits_ok(uint64_t x, uint64_t keep) {
+    constexpr uint64_t H = 0x8080808080808080ull;
+    const uint64_t bad = (x | (x + 0x4646464646464646ull) | ~((x | H) - 0x3030303030303030ull)) & H & keep;
+    return bad == 0;
+}
+// Four digits, the most significant in byte 0 (bytes '0'-'9' or 0):
+// pairs 10 a + b in bytes 0 and 2 (each at most 99: no carries), then
+// 100 x pair0 + pair1.
+__device__ __forceinline__ uint32_t four_digits(uint32_t w) {
+    w &= 0x0F0F0F0Fu;
+    w = w * 10u + (w >> 8);
+    return (w & 0xFFu) * 100u + ((w >> 16) & 0xFFu);
+}
+__device__ __forceinline__ uint32_t eight_digits(uint64_t x) {
+    return four_digits((uint32_t)x) * 10000u + four_digits((uint32_t)(x >> 32));
+}
+
+// 1-8 plain digits at shared offset o (str::parse::<u32> of such a cell).
+__device__ __forceinline__ bool swar_u32(const uint8_t *sd, uint32_t o, uint32_t n, uint32_t &v) {
+    if (n - 1u > 7u) return false;
+    const uint32_t sh = 8u * (8u - n);
+    const uint64_t x = lds_u64(sd, o) << sh;  // the n bytes at the top, zeros below
+    if (!digits_ok(x, ~0ull << sh)) return false;
+    v = eight_digits(x);
     return true;
 }
 
-// [+-]?d{1,3}.d{6}: m / 1e6 correctly rounded (csv_geo.rs:1414-1475).
-__device__ __forceinline__ bool fast_fixed6(const uint8_t *s, uint32_t n, uint64_t &bits) {
-    if (n < 8 || n > 11) return false;
-    const uint8_t c0 = s[0];
-    const uint32_t i = (c0 == '-' || c0 == '+') ? 1u : 0u;
-    if (n - i < 8 || n - i > 10 || s[n - 7] != '.') return false;
-    uint32_t frac = 0, ip = 0;
+// [+-]?d{1,3}.d{6} at shared offset o: the mantissa m (integer and
+// fraction digits) and the f64 bits of m / 1e6, correctly rounded
+// (csv_geo.rs:1414-1475 divides in IEEE arithmetic; Eisel-Lemire gives the
+// same correctly rounded quotient with integer operations).
+__device__ __forceinline__ bool swar_fixed6(const uint8_t *sd, uint32_t o, uint32_t n, uint64_t &bits, uint32_t &m,
+                                            bool &neg) {
+    if (n - 8u > 3u) return false;  // n in [8, 11]
+    const uint32_t c0 = sd[o];
+    const uint32_t sg = (c0 == '-' || c0 == '+') ? 1u : 0u;
+    const uint32_t k = n - 7u - sg;  // integer digits
+    if (k - 1u > 2u) return false;
+    const uint64_t t = lds_u64(sd, o + n - 8u);  // last integer digit, '.', six fraction digits
+    const uint32_t ish = 8u * (4u - k);
+    const uint32_t u = lds_u32(sd, o + sg) << ish;  // the k integer digits at the top
+    if (((uint32_t)(t >> 8) & 0xFFu) != '.' || !digits_ok(t, 0xFFFFFFFFFFFF0000ull) ||
+        !digits_ok(u, (uint64_t)(0xFFFFFFFFu << ish)))
+        return false;
+    m = four_digits(u) * 1000000u + eight_digits(t & 0xFFFFFFFFFFFF0000ull);
+    neg = c0 == '-';
+    bits = dec::eisel_lemire(m, -6) | ((uint64_t)neg << 63);
+    return true;
+}
+
+// An unquoted staged cell copied to dst (any alignment): bytes up to a
+// 4-byte boundary of dst, then aligned word stores, then the tail.
+__device__ __forceinline__ void copy_staged(const uint8_t *sd, uint32_t o, uint32_t n, uint8_t *dst) {
+    uint32_t i = (uint32_t)((4u - ((uintptr_t)dst & 3u)) & 3u);
+    if (i > n) i = n;
+    for (uint32_t k = 0; k < i; k++) dst[k] = sd[o + k];
+    for (; i + 4 <= n; i += 4) *reinterpret_cast<uint32_t *>(dst + i) = lds_u32(sd, o + i);
+    for (; i < n; i++) dst[i] = sd[o + i];
+}
+
+// Select / add on a small per-thread array by a warp-uniform slot without
+// dynamic register indexing (which would move the array to local memory).
+template <typename T, int N>
+__device__ __forceinline__ T pick(const T (&a)[N], int k) {
+    T x = a[0];
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
-        const uint32_t d = (uint32_t)s[n - 6 + k] - '0';
-        if (d > 9) return false;
-        frac = frac * 10 + d;
-    }
-    for (uint32_t k = i; k + 7 < n; k++) {
-        const uint32_t d = (uint32_t)s[k] - '0';
-        if (d > 9) return false;
-        ip = ip * 10 + d;
-    }
-    bits = dec::eisel_lemire((uint64_t)ip * 1000000u + frac, -6) | ((uint64_t)(c0 == '-') << 63);
-    return true;
+    for (int j = 1; j < N; j++) x = k == j ? a[j] : x;
+    return x;
+}
+template <typename T, int N>
+__device__ __forceinline__ void bump(T (&a)[N], int k, T v) {
+#pragma unroll
+    for (int j = 0; j < N; j++) a[j] += k == j ? v : (T)0;
 }
 
-__device__ __noinline__ bool slow_i64(const uint8_t *s, uint32_t n, int64_t &v) {
-    return dec::numeric_view(s, n) && dec::parse_i64(s, n, v);
+// Cells the word-at-a-time paths do not take (other shapes, quoted
+// numbers, cells outside the staged window) go to the general decoders,
+// kept out of line so the per-cell loop stays small. A fast path that
+// accepts a cell gives exactly the general decoder's value.
+// The out-of-line decoders return by value: a local whose address reached
+// a call would live in local memory on the fast path too.
+struct Slow64 {
+    uint64_t v;
+    bool ok;
+};
+__device__ __noinline__ Slow64 slow_i64(const uint8_t *s, uint32_t n) {
+    int64_t v = 0;
+    const bool ok = dec::numeric_view(s, n) && dec::parse_i64(s, n, v);
+    return {(uint64_t)v, ok};
 }
-__device__ __noinline__ bool slow_u32(const uint8_t *s, uint32_t n, uint32_t &v) {
-    return dec::numeric_view(s, n) && dec::parse_u32(s, n, v);
+__device__ __noinline__ Slow64 slow_u32(const uint8_t *s, uint32_t n) {
+    uint32_t v = 0;
+    const bool ok = dec::numeric_view(s, n) && dec::parse_u32(s, n, v);
+    return {v, ok};
 }
-__device__ __noinline__ bool slow_f64(const uint8_t *s, uint32_t n, uint64_t &bits) {
-    double v;
-    if (!(dec::numeric_view(s, n) && dec::parse_f64(s, n, v))) return false;
-    bits = dec::d2u(v);
-    return true;
+__device__ __noinline__ Slow64 slow_f64(const uint8_t *s, uint32_t n) {
+    double v = 0;
+    const bool ok = dec::numeric_view(s, n) && dec::parse_f64(s, n, v);
+    return {dec::d2u(v), ok};
 }
-
-// Count / sum of one f64 cell (csv_geo.rs:1735-1750): values, bit checksum,
-// exact x1e6 sum. The fixed shape needs no general decoder.
-__device__ __noinline__ void stat_slow(StatAcc &a, int k, const uint8_t *s, uint32_t n) { stat_cell(a, k, s, n); }
-__device__ __forceinline__ void stat_value(StatAcc &a, int k, const uint8_t *s, uint32_t n) {
+// One count / sum cell: whether it is a value, its bits, and its exact
+// x1e6 value when it has one.
+struct StatCell {
     uint64_t bits;
-    if (fast_fixed6(s, n, bits)) {
-        // d{1,3}.d{6} is exact in micro-units: +-(ip * 1e6 + frac)
-        const uint32_t i = (s[0] == '-' || s[0] == '+') ? 1u : 0u;
-        int64_t e6 = 0;
-        for (uint32_t q = i; q < n; q++)
-            if (s[q] != '.') e6 = e6 * 10 + (s[q] - '0');
+    int64_t e6;
+    bool value, exact;
+};
+__device__ __noinline__ StatCell stat_slow(const uint8_t *s, uint32_t n) {
+    StatCell r = {0, 0, false, false};
+    double v;
+    if (!dec::numeric_view(s, n) || !dec::parse_f64(s, n, v)) return r;
+    r.value = true;
+    r.bits = dec::d2u(v);
+    r.exact = dec::exact_e6(s, n, r.e6);
+    return r;
+}
+// Count / sum of one f64 cell (csv_geo.rs:1735-1750): values, bit checksum,
+// exact x1e6 sum. The fixed shape is exact in micro-units: +-m.
+__device__ __forceinline__ void stat_value(StatAcc &a, int k, const Win &W, uint32_t from, uint32_t to) {
+    const uint32_t n = to - from;
+    uint64_t bits;
+    uint32_t m, o;
+    bool neg;
+    if (W.staged(from, n, o) && swar_fixed6(W.sdata, o, n, bits, m, neg)) {
         a.values[k]++;
         a.checksum[k] += bits;
-        a.sum_e6[k] += (unsigned long long)(s[0] == '-' ? -e6 : e6);
+        a.sum_e6[k] += neg ? 0ull - (unsigned long long)m : (unsigned long long)m;
         return;
     }
-    stat_slow(a, k, s, n);
+    const StatCell r = stat_slow(W.ptr(from, n), n);
+    if (!r.value) return;
+    a.values[k]++;
+    a.checksum[k] += r.bits;
+    if (r.exact) a.sum_e6[k] += (unsigned long long)r.e6;
+    else a.inexact[k]++;
 }
 
-// A string cell's cleaned bytes into the arena at `at` (bounded by cap);
-// returns the cleaned length. Unquoted cells are copied with byte stores up
-// to a 4-byte boundary of the destination and word stores after it.
-__device__ __forceinline__ uint32_t copy_cell(const uint8_t *s, uint32_t n, uint8_t *arena, uint64_t at,
-                                              uint64_t cap) {
-    if ((n >= 2 && s[0] == '"' && s[n - 1] == '"') || at + n > cap) return copy_clean(s, n, arena, at, cap);
-    uint8_t *dst = arena + at;
-    uint32_t i = 0;
-    const uint32_t head = (uint32_t)((4 - ((uintptr_t)dst & 3)) & 3);
-    for (; i < head && i < n; i++) dst[i] = s[i];
-    for (; i + 4 <= n; i += 4)
-        *reinterpret_cast<uint32_t *>(dst + i) = (uint32_t)s[i] | ((uint32_t)s[i + 1] << 8) |
-                                                 ((uint32_t)s[i + 2] << 16) | ((uint32_t)s[i + 3] << 24);
-    for (; i < n; i++) dst[i] = s[i];
-    return n;
-}
-
-// A non-string cell (I64, U32, F64, BYTES) of row g: stores the value (a
-// zero placeholder when invalid) and returns its validity.
-__device__ __forceinline__ bool decode_value(const RowSpec &rs, int c, uint64_t g, const uint8_t *s, uint32_t n,
-                                             bool present, int64_t from, int64_t to) {
-    const uint32_t ty = rs.type[c];
-    const bool store = g < rs.rows_cap;
-    bool ok = false;
-    if (ty == 0) {
-        int64_t v = 0;
-        if (present) ok = slow_i64(s, n, v);
-        if (store) static_cast<int64_t *>(rs.values[c])[g] = ok ? v : 0;
-    } else if (ty == 1) {
-        uint32_t v = 0;
-        if (present) ok = fast_u32(s, n, v) || slow_u32(s, n, v);
-        if (store) static_cast<uint32_t *>(rs.values[c])[g] = ok ? v : 0u;
-    } else if (ty == 2) {
-        uint64_t bits = 0;
-        if (present) ok = fast_fixed6(s, n, bits) || slow_f64(s, n, bits);
-        if (store) static_cast<uint64_t *>(rs.values[c])[g] = ok ? bits : 0ull;
-    } else {
-        ok = present && n > 0;
-        if (store) {
-            uint32_t *sp = static_cast<uint32_t *>(rs.values[c]);
-            sp[2 * g] = ok ? (uint32_t)from : 0u;
-            sp[2 * g + 1] = ok ? (uint32_t)to : 0u;
-        }
+// Cleaned bytes of all fields of a record (csv_hash.rs:1207-1230): every
+// byte but the separators and a trailing '\r', less what cleaning removes
+// from fields that open with a quote.
+__device__ __forceinline__ uint32_t record_field_bytes(const Win &W, const Rec &x) {
+    uint32_t tot = (x.end2 - x.start) - (x.nf - 1);
+    uint32_t from = x.start;
+    for (uint32_t f = 0; f < x.nf; f++) {
+        const uint32_t to = f + 1 < x.nf ? W.sep(x.sb + f) : x.end2;
+        const uint32_t n = to - from;
+        if (n >= 2 && W.byte(from) == '"') tot -= n - cleaned_len(W.ptr(from, n), n);
+        from = to + 1;
     }
-    return ok;
+    return tot;
 }
 
 template <int D, bool COUNT>
-__global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant__ ColParams p) {
+__global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const __grid_constant__ ColParams p) {
     extern __shared__ __align__(16) uint8_t col_smem_raw[];
     ColSmem &S = *reinterpret_cast<ColSmem *>(col_smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -276,7 +341,7 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
     }
     cp_async_wait_all();
     __syncthreads();
-    const ColView V{p, S};
+    const Win W{S.seps, S.data, p.seps, p.data, (uint32_t)S.sep_lo, S.sep_n, (uint32_t)S.data_lo, S.data_n};
 
     // ---- this thread's records
     Rec rec[kRecPerThread];
@@ -290,22 +355,24 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
         x.nf = 0;
         if (r >= p.n_recs) continue;
         const uint64_t pe = r == 0 ? 0ull : S.ends[li];
-        x.start = r == 0 ? 0 : (int64_t)(uint32_t)pe + 1;
-        x.sb = r == 0 ? 0 : pe >> 32;
+        x.start = r == 0 ? 0u : (uint32_t)pe + 1;
+        x.sb = r == 0 ? 0u : (uint32_t)(pe >> 32);
         // after the last terminator there is a record only if bytes remain
         // (csv_geo.rs:1094-1100)
-        if (r >= p.n_ends && x.start >= (int64_t)p.len) continue;
-        uint64_t se;
+        if (r >= p.n_ends && (uint64_t)x.start >= p.len) continue;
+        uint32_t se;
         if (r < p.n_ends) {
             const uint64_t e = S.ends[li + 1];
-            x.end = (int64_t)(uint32_t)e;
-            se = e >> 32;
+            x.end = (uint32_t)e;
+            se = (uint32_t)(e >> 32);
         } else {
-            x.end = (int64_t)p.len;
-            se = p.n_seps;
+            x.end = (uint32_t)p.len;
+            se = (uint32_t)p.n_seps;
         }
-        x.nf = (uint32_t)(se - x.sb) + 1;
-        x.row = !(D == D_CSV_HASH && x.start < x.end && V.bytes(x.start, x.start + 1)[0] == '#');
+        x.nf = se - x.sb + 1;
+        x.row = !(D == D_CSV_HASH && x.start < x.end && W.byte(x.start) == '#');
+        x.end2 = x.end;
+        if (x.row && x.end > x.start && W.byte(x.end - 1) == '\r') x.end2 = x.end - 1;
         my_rows += x.row;
     }
 
@@ -314,10 +381,11 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
     for (int c = 0; c < rs.ncols; c++) {
         if (rs.type[c] != 3) continue;
         const int k = rs.str_slot[c];
+        const uint32_t f = rs.field[c];
 #pragma unroll
         for (int i = 0; i < kRecPerThread; i++) {
-            int64_t a, b;
-            if (rec[i].row && V.field(rec[i], rs.field[c], a, b)) slen[k] += cleaned_len(V.bytes(a, b), (uint32_t)(b - a));
+            uint32_t a, b;
+            if (rec[i].row && W.field(rec[i], f, a, b)) bump(slen, k, cleaned_len(W.ptr(a, b - a), b - a));
         }
     }
 
@@ -368,55 +436,113 @@ __global__ void __launch_bounds__(kThreads) columns_kernel(const __grid_constant
     if (COUNT) return;
     __syncthreads();
 
-    // ---- cells of this thread's rows
+    // ---- cells of this thread's rows, column by column
     const uint32_t row_base = S.row_base;
     const uint32_t vshift = row_base & 63;
-    uint32_t lrow = S.warp_rows[warp] + ex[0];  // row of the block's rows, block-relative
-    uint64_t at[kMaxStr];
+    const uint32_t lrow0 = S.warp_rows[warp] + ex[0];  // first row of this thread, block-relative
+    uint32_t at[kMaxStr];  // arena offsets (Arrow i32 offsets: below 2^31)
 #pragma unroll
-    for (int k = 0; k < kMaxStr; k++) at[k] = (uint64_t)S.arena_base[k] + S.warp_len[warp][k] + ex[1 + k];
+    for (int k = 0; k < kMaxStr; k++) at[k] = S.arena_base[k] + S.warp_len[warp][k] + ex[1 + k];
     StatAcc acc = {};
     if (rs.rows_cap && blk == 0 && tid == 0)  // string offsets start at 0, rows or not
         for (int c = 0; c < rs.ncols; c++)
             if (rs.type[c] == 3) static_cast<int32_t *>(rs.values[c])[0] = 0;
-    const uint32_t lrow0 = lrow;
+    uint32_t grow[kRecPerThread];  // file row of each record
+    {
+        uint32_t r = row_base + lrow0;
+#pragma unroll
+        for (int i = 0; i < kRecPerThread; i++) {
+            grow[i] = r;
+            r += rec[i].row;
+        }
+    }
     uint32_t okm[kRecPerThread] = {0, 0};  // per record: valid columns
+    for (int c = 0; c < rs.ncols; c++) {
+        const uint32_t f = rs.field[c], ty = rs.type[c];
+#pragma unroll
+        for (int i = 0; i < kRecPerThread; i++) {
+            const Rec &x = rec[i];
+            if (!x.row) continue;
+            const uint32_t g = grow[i];
+            uint32_t a = 0, b = 0, o;
+            const bool present = W.field(x, f, a, b);
+            const uint32_t n = b - a;
+            const bool st = present && W.staged(a, n, o);
+            const bool store = g < rs.rows_cap;
+            bool ok = present;
+            if (ty == 3) {
+                const int k = rs.str_slot[c];
+                const uint32_t pos = pick(at, k);
+                uint32_t len = 0;
+                if (present) {
+                    uint8_t *arena = rs.str_data[c];
+                    if (st && (uint64_t)pos + n <= rs.str_cap[c] &&
+                        !(n >= 2 && W.sdata[o] == '"' && W.sdata[o + n - 1] == '"')) {
+                        copy_staged(W.sdata, o, n, arena + pos);
+                        len = n;
+                    } else {
+                        len = copy_clean(W.ptr(a, n), n, arena, pos, rs.str_cap[c]);
+                    }
+                    bump(at, k, len);
+                }
+                if (store) static_cast<int32_t *>(rs.values[c])[(uint64_t)g + 1] = (int32_t)(pos + len);
+            } else if (ty == 1) {
+                uint32_t v = 0;
+                if (present && !(st && swar_u32(W.sdata, o, n, v))) {
+                    const Slow64 r = slow_u32(W.ptr(a, n), n);
+                    v = (uint32_t)r.v;
+                    ok = r.ok;
+                }
+                if (store) static_cast<uint32_t *>(rs.values[c])[g] = ok ? v : 0u;
+            } else if (ty == 2) {
+                uint64_t bits = 0;
+                uint32_t m;
+                bool neg;
+                if (present && !(st && swar_fixed6(W.sdata, o, n, bits, m, neg))) {
+                    const Slow64 r = slow_f64(W.ptr(a, n), n);
+                    bits = r.v;
+                    ok = r.ok;
+                }
+                if (store) static_cast<uint64_t *>(rs.values[c])[g] = ok ? bits : 0ull;
+            } else if (ty == 0) {
+                int64_t v = 0;
+                uint32_t u;
+                if (present) {
+                    if (st && swar_u32(W.sdata, o, n, u)) v = u;
+                    else {
+                        const Slow64 r = slow_i64(W.ptr(a, n), n);
+                        v = (int64_t)r.v;
+                        ok = r.ok;
+                    }
+                }
+                if (store) static_cast<int64_t *>(rs.values[c])[g] = ok ? v : 0;
+            } else {
+                ok = present && n > 0;
+                if (store) {
+                    uint32_t *sp = static_cast<uint32_t *>(rs.values[c]);
+                    sp[2 * (uint64_t)g] = ok ? a : 0u;
+                    sp[2 * (uint64_t)g + 1] = ok ? b : 0u;
+                }
+            }
+            okm[i] |= (uint32_t)ok << c;
+        }
+    }
 #pragma unroll
     for (int i = 0; i < kRecPerThread; i++) {
         const Rec &x = rec[i];
         if (!x.row) continue;
-        const uint64_t g = (uint64_t)row_base + lrow;
-        for (int c = 0; c < rs.ncols; c++) {
-            int64_t a = 0, b = 0;
-            const bool present = V.field(x, rs.field[c], a, b);
-            const uint32_t n = (uint32_t)(b - a);
-            bool ok;
-            if (rs.type[c] == 3) {
-                const int k = rs.str_slot[c];
-                ok = present;
-                if (present) at[k] += copy_cell(V.bytes(a, b), n, rs.str_data[c], at[k], rs.str_cap[c]);
-                if (g < rs.rows_cap) static_cast<int32_t *>(rs.values[c])[g + 1] = (int32_t)at[k];
-            } else {
-                ok = decode_value(rs, c, g, present ? V.bytes(a, b) : nullptr, n, present, a, b);
-            }
-            okm[i] |= (uint32_t)ok << c;
-        }
         if (rs.want_stats) {
             acc.records++;
+#pragma unroll
             for (int k = 0; k < 2; k++) {
-                int64_t a, b;
-                if (V.field(x, rs.stats_field[k], a, b)) stat_value(acc, k, V.bytes(a, b), (uint32_t)(b - a));
+                uint32_t a, b;
+                if (W.field(x, rs.stats_field[k], a, b)) stat_value(acc, k, W, a, b);
             }
         }
         if (rs.want_fb) {
-            for (uint32_t f = 0; f < x.nf; f++) {
-                int64_t a, b;
-                V.field(x, f, a, b);
-                acc.fields++;
-                acc.bytes += cleaned_len(V.bytes(a, b), (uint32_t)(b - a));
-            }
+            acc.fields += x.nf;
+            acc.bytes += record_field_bytes(W, x);
         }
-        lrow++;
     }
     // validity: the warp's rows are consecutive, at most 64 of them; one
     // 64-bit word per column per warp, OR-reduced across the lanes

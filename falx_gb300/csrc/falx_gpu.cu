@@ -769,7 +769,7 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     if (rc) return rc;
     cp.sums = static_cast<RecSums *>(c->rec_sums);
     // count rows and string bytes per block, scan, then decode
-    const size_t smem_cells = sizeof(ColSmem), smem_count = sizeof(ColSmem) - kDataWin;
+    const size_t smem_cells = sizeof(ColSmem), smem_count = offsetof(ColSmem, data);
 #define FALX_COLS(D)                                                                                           \
     do {                                                                                                       \
         FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D, false>,                                 \

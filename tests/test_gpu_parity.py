@@ -313,3 +313,51 @@ def test_dense_inputs_long_lookback(engine, doc_kind):
         got = engine.parse_columns(doc, fx.Schema(fx.CSV_HASH, cols))
         rows, want = oracle.parse_columns(doc, fx.CSV_HASH, cols)
         compare_columns(got, rows, want, cols)
+
+
+# Cell shapes around the word-at-a-time decoders' boundaries: digit counts
+# 1-10, signs, leading zeros, a non-digit at each position, quoted numbers,
+# the d{1,3}.d{6} shape and its near misses, strings of 0-17 bytes.
+U32_SHAPES = [b"", b"0", b"7", b"42", b"12345678", b"00000001", b"123456789", b"4294967295", b"4294967296",
+              b"99999999999", b"+5", b"-5", b"1a", b"a1", b"1234567a", b"a2345678", b"123 ", b" 123", b'"12"',
+              b'"1"2"', b'""', b"1.0", b"\x80", b"9" * 8, b"/", b":"]
+F64_SHAPES = [b"0.000000", b"-0.000000", b"+0.000001", b"1.500000", b"-172.432059", b"999.999999", b"1000.000000",
+              b"1.5", b"12.3456789", b".123456", b"-.123456", b"1.23456a", b"1a.123456", b"a.123456", b"1.123456e",
+              b"+-1.000000", b"1.1234567", b"12.123456", b"123.12345", b"1e5", b"inf", b"NaN", b'"1.500000"',
+              b"89.999999", b"-90.000000", b"0.0000005", b"1:.123456", b"1/.123456", b"1,5"]
+STR_SHAPES = [b"", b"a", b"ab", b"abc", b"abcd", b"abcde", b"abcdefg", b"abcdefgh", b"abcdefghijklmnopq",
+              b'"a""b"', b'""', b'"', b'x"', b'"x', b'"abc"', b"#x", b"\xff\xfe"]
+SHAPE_COLS = [(0, fx.U32), (1, fx.I64), (2, fx.F64), (3, fx.STR), (4, fx.U32), (5, fx.F64)]
+
+
+def shapes_doc(rng, rows):
+    out = bytearray()
+    for r in range(rows):
+        u = U32_SHAPES[r % len(U32_SHAPES)]
+        f = F64_SHAPES[(r // 3) % len(F64_SHAPES)]
+        s = STR_SHAPES[r % len(STR_SHAPES)]
+        u2 = U32_SHAPES[rng.next() % len(U32_SHAPES)]
+        f2 = F64_SHAPES[rng.next() % len(F64_SHAPES)]
+        out += b",".join([u, u2, f, s, u2, f2])
+        out += b"\r\n" if r % 5 == 0 else b"\n"
+    return bytes(out)
+
+
+@pytest.mark.parametrize("dialect", [fx.CSV, fx.CSV_HASH])
+def test_columns_cell_shapes(engine, dialect):
+    rng = Rng(0x5AA5)
+    for rows in (1, 7, 600, 3000):
+        doc = shapes_doc(rng, rows)
+        got = engine.parse_columns(doc, fx.Schema(dialect, SHAPE_COLS))
+        nrows, want = oracle.parse_columns(doc, dialect, SHAPE_COLS)
+        compare_columns(got, nrows, want, SHAPE_COLS)
+        fb = engine.field_bytes(doc, dialect)
+        assert (fb.fields, fb.bytes) == oracle.field_bytes(doc, dialect)
+        for f0, f1 in ((2, 5), (0, 3)):
+            st = engine.stats_count_sum(doc, dialect, f0, f1)
+            want = oracle.geo_stats(doc, dialect, f0, f1)
+            assert st.records == want.records
+            assert st.values == tuple(want.values)
+            assert st.checksum == tuple(want.checksum)
+            assert st.sum_e6 == tuple(want.sum_e6)
+            assert st.inexact == tuple(want.inexact)
