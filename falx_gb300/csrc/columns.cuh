@@ -57,8 +57,8 @@ struct ColParams {
 // (cells pass) the bytes they span are staged with coalesced loads; what
 // does not fit the windows is read from global memory.
 struct ColSmem {
-    uint64_t ends[kRecBlock + 1];  // ends[r0 - 1 + i]
-    uint32_t seps[kSepWin];
+    alignas(16) uint64_t ends[kRecBlock + 2];  // ends[R0 - 2 + i]: 16-byte copies of even pairs
+    alignas(16) uint32_t seps[kSepWin + 4];    // seps[sep_lo + i], sep_lo a multiple of 4
     uint32_t warp_rows[kWarps];
     uint32_t warp_len[kWarps][kMaxStr];
     uint32_t row_base;
@@ -308,22 +308,31 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
     if (!COUNT)
         for (int i = tid; i < rs.ncols * kRecWords; i += kThreads) S.vbits[i / kRecWords][i % kRecWords] = 0;
 
-    // ---- stage the tape entries of the block's records
-    for (int i = tid; i <= kRecBlock; i += kThreads) {
-        const int64_t e = (int64_t)R0 - 1 + i;
-        if (e >= 0 && (uint64_t)e < p.n_ends) cp_async_ca<8>(&S.ends[i], p.ends + e);
+    // ---- stage the tape entries of the block's records: ends[R0 - 1 ..
+    // R0 + kRecBlock - 1] in 16-byte pairs from the even index R0 - 2
+    const bool al16 = ((uintptr_t)p.ends & 15) == 0 && ((uintptr_t)p.seps & 15) == 0;
+    for (int j = tid; j < (kRecBlock + 2) / 2; j += kThreads) {
+        const int64_t e0 = (int64_t)R0 - 2 + 2 * j;
+        if (al16 && e0 >= 0 && (uint64_t)e0 + 1 < p.n_ends) {
+            cp_async_ca<16>(&S.ends[2 * j], p.ends + e0);
+        } else {
+            if (e0 >= 0 && (uint64_t)e0 < p.n_ends) cp_async_ca<8>(&S.ends[2 * j], p.ends + e0);
+            if (e0 + 1 >= 0 && (uint64_t)(e0 + 1) < p.n_ends) cp_async_ca<8>(&S.ends[2 * j + 1], p.ends + e0 + 1);
+        }
     }
     cp_async_wait_all();
     __syncthreads();
+    const uint64_t *E = S.ends + 1;  // E[i] = ends[R0 - 1 + i]
     if (tid == 0) {
         // separator and byte windows: from the block's first record to its last
         const uint64_t last = (R0 + kRecBlock < p.n_recs ? R0 + kRecBlock : p.n_recs) - 1;
-        const uint64_t sb = R0 == 0 ? 0 : S.ends[0] >> 32;
-        const uint64_t se = last < p.n_ends ? S.ends[last - R0 + 1] >> 32 : p.n_seps;
-        S.sep_lo = sb;
-        S.sep_n = (uint32_t)(se - sb < (uint64_t)kSepWin ? se - sb : (uint64_t)kSepWin);
-        const int64_t lo = R0 == 0 ? 0 : (int64_t)(uint32_t)S.ends[0] + 1;
-        const int64_t hi = last < p.n_ends ? (int64_t)(uint32_t)S.ends[last - R0 + 1] : (int64_t)p.len;
+        const uint64_t sb = R0 == 0 ? 0 : E[0] >> 32;
+        const uint64_t se = last < p.n_ends ? E[last - R0 + 1] >> 32 : p.n_seps;
+        const uint64_t sb4 = al16 ? sb & ~3ull : sb;  // 16-byte aligned start
+        S.sep_lo = sb4;
+        S.sep_n = (uint32_t)(sb - sb4) + (uint32_t)(se - sb < (uint64_t)kSepWin ? se - sb : (uint64_t)kSepWin);
+        const int64_t lo = R0 == 0 ? 0 : (int64_t)(uint32_t)E[0] + 1;
+        const int64_t hi = last < p.n_ends ? (int64_t)(uint32_t)E[last - R0 + 1] : (int64_t)p.len;
         const int64_t q0 = (lo + p.shift) & ~15ll;  // 16-byte aligned address offset
         const int64_t qend = (int64_t)((p.shift + p.len + 15) & ~15ull);
         int64_t qn = ((hi + p.shift + 15) & ~15ll) - q0;
@@ -334,7 +343,22 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
         S.data_n = COUNT ? 0u : (uint32_t)qn;  // the count pass reads its few bytes in place
     }
     __syncthreads();
-    for (uint32_t i = tid; i < S.sep_n; i += kThreads) cp_async_ca<4>(&S.seps[i], p.seps + S.sep_lo + i);
+    {
+        const uint32_t sn = S.sep_n;
+        const uint64_t sl = S.sep_lo;
+        if (al16) {
+            for (uint32_t j = tid; 4 * j < sn; j += kThreads) {
+                const uint64_t i0 = sl + 4 * j;
+                if (i0 + 3 < p.n_seps) {
+                    cp_async_ca<16>(&S.seps[4 * j], p.seps + i0);
+                } else {
+                    for (uint32_t q = 0; q < 4 && i0 + q < p.n_seps; q++) cp_async_ca<4>(&S.seps[4 * j + q], p.seps + i0 + q);
+                }
+            }
+        } else {
+            for (uint32_t i = tid; i < sn; i += kThreads) cp_async_ca<4>(&S.seps[i], p.seps + sl + i);
+        }
+    }
     if (!COUNT) {
         const uint8_t *src = p.abase + (S.data_lo + p.shift);
         for (uint32_t i = tid; i < S.data_n / 16; i += kThreads) cp_async_ca<16>(S.data + 16 * i, src + 16 * i);
@@ -349,12 +373,12 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
 #pragma unroll
     for (int i = 0; i < kRecPerThread; i++) {
         const uint64_t r = R0 + (uint64_t)tid * kRecPerThread + i;
-        const int li = tid * kRecPerThread + i;  // S.ends[li] = ends[r - 1]
+        const int li = tid * kRecPerThread + i;  // E[li] = ends[r - 1]
         Rec &x = rec[i];
         x.row = false;
         x.nf = 0;
         if (r >= p.n_recs) continue;
-        const uint64_t pe = r == 0 ? 0ull : S.ends[li];
+        const uint64_t pe = r == 0 ? 0ull : E[li];
         x.start = r == 0 ? 0u : (uint32_t)pe + 1;
         x.sb = r == 0 ? 0u : (uint32_t)(pe >> 32);
         // after the last terminator there is a record only if bytes remain
@@ -362,7 +386,7 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
         if (r >= p.n_ends && (uint64_t)x.start >= p.len) continue;
         uint32_t se;
         if (r < p.n_ends) {
-            const uint64_t e = S.ends[li + 1];
+            const uint64_t e = E[li + 1];
             x.end = (uint32_t)e;
             se = (uint32_t)(e >> 32);
         } else {

@@ -292,40 +292,48 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
         __syncthreads();
     }
     ce += S.warp_c[warp];
+    // Stage the thread's structurals (tile offset, bit 15 = terminator). A
+    // warp's threads are consecutive, so its entries are one contiguous run
+    // of the staging list and the warp writes index, separators and ends
+    // from it alone, coalesced, after a warp barrier.
     {
         uint32_t k = cfield(ce, 0);
         uint64_t mm = stm;
         while (mm) {
             const unsigned bpos = __ffsll((long long)mm) - 1;
-            if (k < (uint32_t)kTile) S.stage[k] = (uint16_t)(tid * kThreadBytes + bpos);
+            if (k < (uint32_t)kTile)
+                S.stage[k] = (uint16_t)(tid * kThreadBytes + bpos) | (uint16_t)(((term >> bpos) & 1) << 15);
             k++;
             mm &= mm - 1;
         }
     }
-    __syncthreads();
-    const uint32_t n_tile = min(cfield(S.tile_c, 0), (uint32_t)kTile);
-    if (p.index) {
-        for (uint32_t i = tid; i < n_tile; i += kThreads) {
-            const uint64_t g = (uint64_t)pre[0] + i;
-            if (g < p.index_cap) p.index[g] = (uint32_t)(p.pos_base + vs + S.stage[i]);
-        }
-    }
-    if (p.seps || p.ends) {
-        const uint32_t my_s = cfield(ce, 0), my_t = cfield(ce, 1);
-        uint64_t sep_before = (uint64_t)(pre[0] - pre[1]) + (my_s - my_t);
-        uint64_t term_before = (uint64_t)pre[1] + my_t;
-        uint64_t mm = stm;
-        while (mm) {
-            const unsigned bpos = __ffsll((long long)mm) - 1;
-            const uint64_t pos = (uint64_t)(p.pos_base + L.base_t + bpos);
-            if ((term >> bpos) & 1) {
-                if (p.ends && term_before < p.ends_cap) p.ends[term_before] = ((p.sep_base + sep_before) << 32) | pos;
-                term_before++;
-            } else {
-                if (p.seps && sep_before < p.seps_cap) p.seps[sep_before] = (uint32_t)pos;
-                sep_before++;
+    __syncwarp();
+    {
+        const unsigned long long cend = ce + c;  // the thread's inclusive counts
+        const uint32_t k0 = cfield(__shfl_sync(0xffffffffu, ce, 0), 0);
+        const uint32_t k1 = min(cfield(__shfl_sync(0xffffffffu, cend, 31), 0), (uint32_t)kTile);
+        uint32_t t = cfield(__shfl_sync(0xffffffffu, ce, 0), 1);  // tile terminators before the chunk
+        const uint32_t lt = (1u << lane) - 1u;
+        const bool tape = p.seps || p.ends;
+        for (uint32_t k = k0; k < k1; k += 32) {
+            const uint32_t kk = k + lane;
+            const bool in = kk < k1;
+            const uint32_t e = in ? S.stage[kk] : 0u;
+            const bool is_t = in && (e >> 15);
+            const uint32_t bt = __ballot_sync(0xffffffffu, is_t);
+            const uint64_t gs = (uint64_t)pre[0] + kk;                     // structural ordinal
+            const uint64_t gt = (uint64_t)pre[1] + t + __popc(bt & lt);    // terminators before it
+            const uint32_t pos = (uint32_t)(p.pos_base + vs + (e & 0x7FFFu));
+            if (in && p.index && gs < p.index_cap) p.index[gs] = pos;
+            if (in && tape) {
+                const uint64_t gsep = gs - gt;  // separators before it
+                if (is_t) {
+                    if (p.ends && gt < p.ends_cap) p.ends[gt] = ((p.sep_base + gsep) << 32) | pos;
+                } else if (p.seps && gsep < p.seps_cap) {
+                    p.seps[gsep] = pos;
+                }
             }
-            mm &= mm - 1;
+            t += __popc(bt);
         }
     }
 }
