@@ -367,16 +367,19 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
     __syncthreads();
     const Win W{S.seps, S.data, p.seps, p.data, (uint32_t)S.sep_lo, S.sep_n, (uint32_t)S.data_lo, S.data_n};
 
-    // ---- this thread's records
+    // ---- this thread's records: warp w owns records [64 w, 64 w + 64) of
+    // the block and lane L takes records L and L + 32 of them, so a warp's
+    // loads, value stores and validity ballots each cover 32 consecutive
+    // records
     Rec rec[kRecPerThread];
-    uint32_t my_rows = 0;
 #pragma unroll
     for (int i = 0; i < kRecPerThread; i++) {
-        const uint64_t r = R0 + (uint64_t)tid * kRecPerThread + i;
-        const int li = tid * kRecPerThread + i;  // E[li] = ends[r - 1]
+        const int li = warp * 64 + i * 32 + lane;  // E[li] = ends[r - 1]
+        const uint64_t r = R0 + (uint64_t)li;
         Rec &x = rec[i];
         x.row = false;
         x.nf = 0;
+        x.start = x.end = x.end2 = x.sb = 0;
         if (r >= p.n_recs) continue;
         const uint64_t pe = r == 0 ? 0ull : E[li];
         x.start = r == 0 ? 0u : (uint32_t)pe + 1;
@@ -397,11 +400,17 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
         x.row = !(D == D_CSV_HASH && x.start < x.end && W.byte(x.start) == '#');
         x.end2 = x.end;
         if (x.row && x.end > x.start && W.byte(x.end - 1) == '\r') x.end2 = x.end - 1;
-        my_rows += x.row;
     }
 
-    // ---- string cell lengths
-    uint32_t slen[kMaxStr] = {0, 0, 0, 0};
+    // ---- per record: row (0/1) and cleaned bytes of each string slot
+    const int nv = 1 + rs.nstr;  // values scanned: rows, then string slots
+    uint32_t v[kRecPerThread][1 + kMaxStr];
+#pragma unroll
+    for (int i = 0; i < kRecPerThread; i++) {
+        v[i][0] = rec[i].row;
+#pragma unroll
+        for (int k = 1; k < 1 + kMaxStr; k++) v[i][k] = 0;
+    }
     for (int c = 0; c < rs.ncols; c++) {
         if (rs.type[c] != 3) continue;
         const int k = rs.str_slot[c];
@@ -409,25 +418,36 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
 #pragma unroll
         for (int i = 0; i < kRecPerThread; i++) {
             uint32_t a, b;
-            if (rec[i].row && W.field(rec[i], f, a, b)) bump(slen, k, cleaned_len(W.ptr(a, b - a), b - a));
+            if (rec[i].row && W.field(rec[i], f, a, b)) {
+                const uint32_t l = cleaned_len(W.ptr(a, b - a), b - a);
+#pragma unroll
+                for (int j = 0; j < kMaxStr; j++) v[i][1 + j] += j == k ? l : 0u;
+            }
         }
     }
 
-    // ---- block scan of (rows, string bytes)
-    uint32_t v[1 + kMaxStr] = {my_rows, slen[0], slen[1], slen[2], slen[3]};
-    uint32_t ex[1 + kMaxStr];
+    // ---- exclusive prefixes in record order: a warp's records 0-31 (i = 0)
+    // come before 32-63 (i = 1); then warps in order
+    uint32_t ex[kRecPerThread][1 + kMaxStr];
 #pragma unroll
     for (int k = 0; k < 1 + kMaxStr; k++) {
-        uint32_t x = v[k];
+        if (k >= nv) break;
+        uint32_t x0 = v[0][k], x1 = v[1][k];
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t o = __shfl_up_sync(0xffffffffu, x, d);
-            if (lane >= d) x += o;
+            const uint32_t o0 = __shfl_up_sync(0xffffffffu, x0, d);
+            const uint32_t o1 = __shfl_up_sync(0xffffffffu, x1, d);
+            if (lane >= d) {
+                x0 += o0;
+                x1 += o1;
+            }
         }
-        ex[k] = x - v[k];
+        const uint32_t t0 = __shfl_sync(0xffffffffu, x0, 31);
+        ex[0][k] = x0 - v[0][k];
+        ex[1][k] = t0 + x1 - v[1][k];
         if (lane == 31) {
-            if (k == 0) S.warp_rows[warp] = x;
-            else S.warp_len[warp][k - 1] = x;
+            if (k == 0) S.warp_rows[warp] = t0 + x1;
+            else S.warp_len[warp][k - 1] = t0 + x1;
         }
     }
     __syncthreads();
@@ -435,6 +455,7 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
         // warp prefixes and block totals
 #pragma unroll
         for (int k = 0; k < 1 + kMaxStr; k++) {
+            if (k >= nv) break;
             const uint32_t w = lane < kWarps ? (k == 0 ? S.warp_rows[lane] : S.warp_len[lane][k - 1]) : 0u;
             uint32_t x = w;
 #pragma unroll
@@ -451,6 +472,8 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
                 else p.sums[blk].arena[k - 1] = x;
             }
         }
+        if (COUNT && lane == 0)
+            for (int k = nv - 1; k < kMaxStr; k++) p.sums[blk].arena[k] = 0;
         if (!COUNT && lane == 0) {
             S.row_base = p.sums[blk].rows;
 #pragma unroll
@@ -460,34 +483,27 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
     if (COUNT) return;
     __syncthreads();
 
-    // ---- cells of this thread's rows, column by column
+    // ---- cells, column by column
     const uint32_t row_base = S.row_base;
-    const uint32_t vshift = row_base & 63;
-    const uint32_t lrow0 = S.warp_rows[warp] + ex[0];  // first row of this thread, block-relative
-    uint32_t at[kMaxStr];  // arena offsets (Arrow i32 offsets: below 2^31)
+    const uint32_t wrow = S.warp_rows[warp];  // the warp's first row, block-relative
+    uint32_t grow[kRecPerThread];             // file row of each record
 #pragma unroll
-    for (int k = 0; k < kMaxStr; k++) at[k] = S.arena_base[k] + S.warp_len[warp][k] + ex[1 + k];
-    StatAcc acc = {};
+    for (int i = 0; i < kRecPerThread; i++) grow[i] = row_base + wrow + ex[i][0];
     if (rs.rows_cap && blk == 0 && tid == 0)  // string offsets start at 0, rows or not
         for (int c = 0; c < rs.ncols; c++)
             if (rs.type[c] == 3) static_cast<int32_t *>(rs.values[c])[0] = 0;
-    uint32_t grow[kRecPerThread];  // file row of each record
-    {
-        uint32_t r = row_base + lrow0;
-#pragma unroll
-        for (int i = 0; i < kRecPerThread; i++) {
-            grow[i] = r;
-            r += rec[i].row;
-        }
-    }
     uint32_t okm[kRecPerThread] = {0, 0};  // per record: valid columns
     for (int c = 0; c < rs.ncols; c++) {
         const uint32_t f = rs.field[c], ty = rs.type[c];
-#pragma unroll
+        const int k = rs.str_slot[c];
+        const uint32_t abase = ty == 3 ? S.arena_base[k] + S.warp_len[warp][k] : 0u;
+        // one copy of the cell code for both records (a smaller loop body
+        // measured faster than the unrolled pair: instruction fetch)
+#pragma unroll 1
         for (int i = 0; i < kRecPerThread; i++) {
-            const Rec &x = rec[i];
+            const Rec x = i ? rec[1] : rec[0];
             if (!x.row) continue;
-            const uint32_t g = grow[i];
+            const uint32_t g = i ? grow[1] : grow[0];
             uint32_t a = 0, b = 0, o;
             const bool present = W.field(x, f, a, b);
             const uint32_t n = b - a;
@@ -495,8 +511,8 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
             const bool store = g < rs.rows_cap;
             bool ok = present;
             if (ty == 3) {
-                const int k = rs.str_slot[c];
-                const uint32_t pos = pick(at, k);
+                // arena offset of this record's cell (Arrow i32 offsets: below 2^31)
+                const uint32_t pos = abase + (i ? pick(ex[1], 1 + k) : pick(ex[0], 1 + k));
                 uint32_t len = 0;
                 if (present) {
                     uint8_t *arena = rs.str_data[c];
@@ -507,7 +523,6 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
                     } else {
                         len = copy_clean(W.ptr(a, n), n, arena, pos, rs.str_cap[c]);
                     }
-                    bump(at, k, len);
                 }
                 if (store) static_cast<int32_t *>(rs.values[c])[(uint64_t)g + 1] = (int32_t)(pos + len);
             } else if (ty == 1) {
@@ -548,12 +563,15 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
                     sp[2 * (uint64_t)g + 1] = ok ? b : 0u;
                 }
             }
-            okm[i] |= (uint32_t)ok << c;
+            if (i) okm[1] |= (uint32_t)ok << c;
+            else okm[0] |= (uint32_t)ok << c;
         }
     }
-#pragma unroll
+    StatAcc acc = {};
+    uint32_t fb_fields = 0, fb_bytes = 0;  // below 2^32: the input is shorter than 4 GiB
+#pragma unroll 1
     for (int i = 0; i < kRecPerThread; i++) {
-        const Rec &x = rec[i];
+        const Rec x = i ? rec[1] : rec[0];
         if (!x.row) continue;
         if (rs.want_stats) {
             acc.records++;
@@ -564,29 +582,60 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
             }
         }
         if (rs.want_fb) {
-            acc.fields += x.nf;
-            acc.bytes += record_field_bytes(W, x);
+            fb_fields += x.nf;
+            fb_bytes += record_field_bytes(W, x);
         }
     }
-    // validity: the warp's rows are consecutive, at most 64 of them; one
-    // 64-bit word per column per warp, OR-reduced across the lanes
-    {
-        const uint32_t wr = S.warp_rows[warp];  // the warp's first row, block-relative
-        const uint32_t ro = lrow0 - wr;         // this lane's first row within the warp
-        for (int c = 0; c < rs.ncols; c++) {
-            uint64_t mine = 0;
-            uint32_t k = 0;
+
+    // ---- field-byte and count / sum totals: warp sums into shared memory
+    // (read after the barrier below), one global atomic per value and block
+    const int nred = rs.want_stats ? 11 : rs.want_fb ? 2 : 0;
+    if (nred) {
+        unsigned long long r[11] = {fb_fields, fb_bytes, acc.records, acc.values[0], acc.values[1], acc.checksum[0],
+                                    acc.checksum[1], acc.sum_e6[0], acc.sum_e6[1], acc.inexact[0], acc.inexact[1]};
+        if (nred == 2) {
+            uint32_t f = fb_fields, by = fb_bytes;
 #pragma unroll
-            for (int i = 0; i < kRecPerThread; i++) {
-                if (!rec[i].row) continue;
-                mine |= (uint64_t)((okm[i] >> c) & 1u) << (ro + k);
-                k++;
+            for (int d = 16; d > 0; d >>= 1) {
+                f += __shfl_down_sync(0xffffffffu, f, d);
+                by += __shfl_down_sync(0xffffffffu, by, d);
             }
-            const uint32_t lo = __reduce_or_sync(0xffffffffu, (uint32_t)mine);
-            const uint32_t hi = __reduce_or_sync(0xffffffffu, (uint32_t)(mine >> 32));
-            if (lane == 0 && (lo | hi)) {
-                const uint64_t word = (uint64_t)lo | ((uint64_t)hi << 32);
-                const uint32_t lb = vshift + wr;
+            r[0] = f;
+            r[1] = by;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 11; k++) {
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) r[k] += __shfl_down_sync(0xffffffffu, r[k], d);
+            }
+        }
+        if (lane == 0)
+            for (int k = 0; k < nred; k++) S.red[warp][k] = r[k];
+    }
+
+    // ---- validity: the warp's rows are consecutive, at most 64 of them;
+    // one 64-bit word per column and warp. With every record a row, record
+    // L + 32 i of the warp is its row L + 32 i and the word is two ballots;
+    // otherwise rows are ranked within the warp and the bits OR-reduced.
+    {
+        const uint32_t rm0 = __ballot_sync(0xffffffffu, rec[0].row), rm1 = __ballot_sync(0xffffffffu, rec[1].row);
+        const bool dense = (rm0 & rm1) == 0xffffffffu;
+        const uint32_t lt = (1u << lane) - 1u;
+        const uint32_t r0 = __popc(rm0 & lt), r1 = __popc(rm0) + __popc(rm1 & lt);  // row ranks
+        const uint32_t lb = (row_base & 63) + wrow;
+        for (int c = 0; c < rs.ncols; c++) {
+            uint64_t word;
+            if (dense) {
+                word = (uint64_t)__ballot_sync(0xffffffffu, (okm[0] >> c) & 1u) |
+                       ((uint64_t)__ballot_sync(0xffffffffu, (okm[1] >> c) & 1u) << 32);
+            } else {
+                uint64_t mine = 0;
+                if (rec[0].row) mine |= (uint64_t)((okm[0] >> c) & 1u) << r0;
+                if (rec[1].row) mine |= (uint64_t)((okm[1] >> c) & 1u) << r1;
+                word = (uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)mine) |
+                       ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(mine >> 32)) << 32);
+            }
+            if (lane == 0 && word) {
                 atomicOr((unsigned long long *)&S.vbits[c][lb >> 6], (unsigned long long)(word << (lb & 63)));
                 if (lb & 63) atomicOr((unsigned long long *)&S.vbits[c][(lb >> 6) + 1],
                                       (unsigned long long)(word >> (64 - (lb & 63))));
@@ -606,25 +655,13 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
         }
     }
 
-    // ---- field bytes and count / sum totals
-    if (rs.want_fb || rs.want_stats) {
-        unsigned long long r[11] = {acc.fields, acc.bytes, acc.records, acc.values[0], acc.values[1],
-                                    acc.checksum[0], acc.checksum[1], acc.sum_e6[0], acc.sum_e6[1],
-                                    acc.inexact[0], acc.inexact[1]};
-#pragma unroll
-        for (int k = 0; k < 11; k++) {
-#pragma unroll
-            for (int d = 16; d > 0; d >>= 1) r[k] += __shfl_down_sync(0xffffffffu, r[k], d);
-            if (lane == 0) S.red[warp][k] = r[k];
-        }
-        __syncthreads();
-        if (tid < 11) {
-            unsigned long long t = 0;
-            for (int w = 0; w < kWarps; w++) t += S.red[w][tid];
-            if (t) {
-                if (tid < 2) atomicAdd(tid == 0 ? &p.hdr->fb_fields : &p.hdr->fb_bytes, t);
-                else atomicAdd(&p.hdr->st_records + (tid - 2), t);
-            }
+    // ---- block totals
+    if (tid < nred) {
+        unsigned long long t = 0;
+        for (int w = 0; w < kWarps; w++) t += S.red[w][tid];
+        if (t) {
+            if (tid < 2) atomicAdd(tid == 0 ? &p.hdr->fb_fields : &p.hdr->fb_bytes, t);
+            else atomicAdd(&p.hdr->st_records + (tid - 2), t);
         }
     }
 }
