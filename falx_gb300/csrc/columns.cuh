@@ -4,17 +4,15 @@
 // terminated record `(separators before << 32) | terminator offset` in
 // `ends` (csv_geo.rs:1838-1849 push_tape). A record's fields are then a
 // contiguous run of `seps`, so every record can be decoded independently.
-// Three launches, none of which waits on another CTA:
-//  1. count: one CTA per 512 consecutive records (two per thread) counts
-//     its rows (csv_hash comment records are not rows, csv_hash.rs:1381) and
-//     the cleaned bytes of its string cells;
-//  2. scan: one CTA turns those per-block sums into exclusive prefixes;
-//  3. cells: the same blocks again, now knowing the rows and arena bytes
-//     before them, decode their cells (ColumnSink semantics,
-//     csv_geo.rs:952-1101; decoders csv_geo.rs:1313-1486,
-//     csv_hash.rs:1688-1791), write values, validity, string offsets and
-//     bytes, and add their field-byte and count/sum totals
-//     (csv_hash.rs:1095-1230, csv_geo.rs:1605-1770).
+// One launch: CTA b owns the 512 records [512 b, 512 b + 512). It stages
+// their tape entries and bytes, counts its rows (csv_hash comment records
+// are not rows, csv_hash.rs:1381) and the cleaned bytes of its string
+// cells, publishes those sums, and finds the sums of the blocks before it
+// with a decoupled look-back (one warp, bounded waits); then it decodes its
+// cells (ColumnSink semantics, csv_geo.rs:952-1101; decoders
+// csv_geo.rs:1313-1486, csv_hash.rs:1688-1791), writes values, validity,
+// string offsets and bytes, and adds its field-byte and count/sum totals
+// (csv_hash.rs:1095-1230, csv_geo.rs:1605-1770).
 #pragma once
 
 #include <cstdint>
@@ -32,10 +30,16 @@ constexpr int kRecWords = kRecBlock / 64 + 1;        // validity words a block's
 constexpr int kSepWin = 3072;                        // separators staged per CTA
 constexpr int kDataWin = 32768;                      // bytes staged per CTA (cells pass)
 
-struct RecSums {  // one per record block: rows and string-arena bytes
+// Look-back record of one record block, tagged with the call's epoch:
+// flag = epoch * 4 + 1 once the block's own sums are published, + 2 once
+// the sums up to and including it are.
+struct BlkStatus {
+    uint32_t flag;
     uint32_t rows;
     uint32_t arena[kMaxStr];
-    uint32_t pad[3];
+    uint32_t incl_rows;
+    uint32_t pad;
+    unsigned long long incl_arena[kMaxStr];
 };
 
 struct ColParams {
@@ -48,7 +52,9 @@ struct ColParams {
     const uint64_t *ends;
     uint64_t n_ends;
     uint64_t n_recs;  // n_ends, plus one for a trailing record without terminator
-    RecSums *sums;    // per block: its sums (count), then the sums before it (cells)
+    BlkStatus *status;  // per record block
+    uint32_t epoch;
+    uint32_t n_blocks;
     DevHeader *hdr;
     RowSpec rows;
 };
@@ -69,8 +75,7 @@ struct ColSmem {
     uint32_t data_n;
     uint64_t vbits[kMaxCols][kRecWords];
     unsigned long long red[kWarps][12];
-    alignas(16) uint8_t data[kDataWin + 16];  // last: the count pass launches without it; 16 bytes of
-                                              // slack for word reads that start near the window end
+    alignas(16) uint8_t data[kDataWin + 16];  // 16 bytes of slack for word reads near the window end
 };
 
 // Asynchronous global -> shared copies (all of a CTA's copies in flight at
@@ -297,16 +302,15 @@ __device__ __forceinline__ uint32_t record_field_bytes(const Win &W, const Rec &
     return tot;
 }
 
-template <int D, bool COUNT>
-__global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const __grid_constant__ ColParams p) {
+template <int D>
+__global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_constant__ ColParams p) {
     extern __shared__ __align__(16) uint8_t col_smem_raw[];
     ColSmem &S = *reinterpret_cast<ColSmem *>(col_smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const RowSpec &rs = p.rows;
     const uint32_t blk = blockIdx.x;
     const uint64_t R0 = (uint64_t)blk * kRecBlock;
-    if (!COUNT)
-        for (int i = tid; i < rs.ncols * kRecWords; i += kThreads) S.vbits[i / kRecWords][i % kRecWords] = 0;
+    for (int i = tid; i < rs.ncols * kRecWords; i += kThreads) S.vbits[i / kRecWords][i % kRecWords] = 0;
 
     // ---- stage the tape entries of the block's records: ends[R0 - 1 ..
     // R0 + kRecBlock - 1] in 16-byte pairs from the even index R0 - 2
@@ -340,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
         if (qn > kDataWin) qn = kDataWin;
         if (qn < 0) qn = 0;
         S.data_lo = q0 - p.shift;
-        S.data_n = COUNT ? 0u : (uint32_t)qn;  // the count pass reads its few bytes in place
+        S.data_n = (uint32_t)qn;
     }
     __syncthreads();
     {
@@ -359,7 +363,7 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
             for (uint32_t i = tid; i < sn; i += kThreads) cp_async_ca<4>(&S.seps[i], p.seps + sl + i);
         }
     }
-    if (!COUNT) {
+    {
         const uint8_t *src = p.abase + (S.data_lo + p.shift);
         for (uint32_t i = tid; i < S.data_n / 16; i += kThreads) cp_async_ca<16>(S.data + 16 * i, src + 16 * i);
     }
@@ -453,6 +457,7 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
     __syncthreads();
     if (warp == 0) {
         // warp prefixes and block totals
+        uint32_t tot[1 + kMaxStr] = {0, 0, 0, 0, 0};
 #pragma unroll
         for (int k = 0; k < 1 + kMaxStr; k++) {
             if (k >= nv) break;
@@ -467,20 +472,76 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
                 if (k == 0) S.warp_rows[lane] = x - w;
                 else S.warp_len[lane][k - 1] = x - w;
             }
-            if (COUNT && lane == 31) {
-                if (k == 0) p.sums[blk].rows = x;
-                else p.sums[blk].arena[k - 1] = x;
+            tot[k] = __shfl_sync(0xffffffffu, x, 31);
+        }
+        // publish the block's sums, then add up those of the blocks before it
+        BlkStatus *me = p.status + blk;
+        if (lane == 0) {
+            me->rows = tot[0];
+#pragma unroll
+            for (int k = 0; k < kMaxStr; k++) me->arena[k] = tot[1 + k];
+            st_release(&me->flag, p.epoch * 4 + 1);
+        }
+        unsigned long long pre[1 + kMaxStr] = {0, 0, 0, 0, 0};
+        const uint64_t t0 = globaltimer_ns();
+        for (int64_t hi = (int64_t)blk - 1; hi >= 0; hi -= 32) {
+            // lane l watches block hi - l: wait until no block nearer than
+            // the nearest inclusive prefix is still unpublished
+            const int64_t j = hi - lane;
+            uint32_t fi;
+            for (uint32_t it = 0;; it++) {
+                const uint32_t flag = j >= 0 ? ld_acquire(&p.status[j].flag) : 0u;
+                const bool cur = (flag >> 2) == p.epoch;
+                const uint32_t bi = __ballot_sync(0xffffffffu, j >= 0 && cur && (flag & 3) >= 2);
+                const uint32_t bm = __ballot_sync(0xffffffffu, j >= 0 && !(cur && (flag & 3) >= 1));
+                fi = bi ? __ffs(bi) - 1 : 32u;
+                const uint32_t fm = bm ? __ffs(bm) - 1 : 32u;
+                if (fm > fi || bm == 0) break;
+                if ((it & 15) == 15) {
+                    const bool stop = lane == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
+                    if (__any_sync(0xffffffffu, stop)) {
+                        if (lane == 0) fail(p.hdr, ERR_TIMEOUT);
+                        fi = 0;
+                        hi = -1;
+                        break;
+                    }
+                }
+                __nanosleep(64);
+            }
+            if (hi < 0) break;
+            unsigned long long v[1 + kMaxStr] = {0, 0, 0, 0, 0};
+            if ((uint32_t)lane < fi && j >= 0) {
+                v[0] = p.status[j].rows;
+#pragma unroll
+                for (int k = 0; k < kMaxStr; k++) v[1 + k] = p.status[j].arena[k];
+            } else if ((uint32_t)lane == fi) {
+                v[0] = p.status[j].incl_rows;
+#pragma unroll
+                for (int k = 0; k < kMaxStr; k++) v[1 + k] = p.status[j].incl_arena[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 1 + kMaxStr; k++) {
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], d);
+                pre[k] += v[k];
+            }
+            if (fi < 32) break;
+        }
+        if (lane == 0) {
+            me->incl_rows = (uint32_t)(pre[0] + tot[0]);
+#pragma unroll
+            for (int k = 0; k < kMaxStr; k++) me->incl_arena[k] = pre[1 + k] + tot[1 + k];
+            st_release(&me->flag, p.epoch * 4 + 2);
+            S.row_base = (uint32_t)pre[0];
+#pragma unroll
+            for (int k = 0; k < kMaxStr; k++) S.arena_base[k] = (uint32_t)pre[1 + k];  // i32 offsets: checked on the host
+            if (blk == p.n_blocks - 1) {
+                p.hdr->n_rows = pre[0] + tot[0];
+#pragma unroll
+                for (int k = 0; k < kMaxStr; k++) p.hdr->arena[k] = pre[1 + k] + tot[1 + k];
             }
         }
-        if (COUNT && lane == 0)
-            for (int k = nv - 1; k < kMaxStr; k++) p.sums[blk].arena[k] = 0;
-        if (!COUNT && lane == 0) {
-            S.row_base = p.sums[blk].rows;
-#pragma unroll
-            for (int k = 0; k < kMaxStr; k++) S.arena_base[k] = p.sums[blk].arena[k];
-        }
     }
-    if (COUNT) return;
     __syncthreads();
 
     // ---- cells, column by column
@@ -668,72 +729,3 @@ __global__ void __launch_bounds__(kThreads, COUNT ? 6 : 4) columns_kernel(const 
 
 }  // namespace falx
 
-namespace falx {
-
-// Exclusive prefixes of the per-block sums, and the totals. One CTA of
-// 1024 threads; warp w owns a contiguous run of blocks and reads it 32
-// entries at a time (coalesced): first its total, then, after a scan of the
-// 32 totals, the prefixes.
-__global__ void __launch_bounds__(1024) columns_scan(RecSums *sums, uint32_t n, DevHeader *hdr) {
-    __shared__ unsigned long long wsum[32][1 + kMaxStr];
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const uint32_t per = (n + 31) / 32, lo = min(n, warp * per), hi = min(n, lo + per);
-    unsigned long long tot[1 + kMaxStr] = {0, 0, 0, 0, 0};
-    for (uint32_t i = lo + lane; i < hi; i += 32) {
-        const RecSums v = sums[i];
-        tot[0] += v.rows;
-#pragma unroll
-        for (int k = 0; k < kMaxStr; k++) tot[1 + k] += v.arena[k];
-    }
-#pragma unroll
-    for (int k = 0; k < 1 + kMaxStr; k++) {
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) tot[k] += __shfl_xor_sync(0xffffffffu, tot[k], d);
-        if (lane == 0) wsum[warp][k] = tot[k];
-    }
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int k = 0; k < 1 + kMaxStr; k++) {
-            const unsigned long long w = wsum[lane][k];
-            unsigned long long x = w;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const unsigned long long o = __shfl_up_sync(0xffffffffu, x, d);
-                if (lane >= d) x += o;
-            }
-            wsum[lane][k] = x - w;
-            if (lane == 31) {
-                if (k == 0) hdr->n_rows = x;
-                else hdr->arena[k - 1] = x;
-            }
-        }
-    }
-    __syncthreads();
-    unsigned long long carry[1 + kMaxStr];
-#pragma unroll
-    for (int k = 0; k < 1 + kMaxStr; k++) carry[k] = wsum[warp][k];
-    for (uint32_t i0 = lo; i0 < hi; i0 += 32) {
-        const uint32_t i = i0 + lane;
-        RecSums v = {};
-        if (i < hi) v = sums[i];
-        uint32_t val[1 + kMaxStr] = {v.rows, v.arena[0], v.arena[1], v.arena[2], v.arena[3]};
-#pragma unroll
-        for (int k = 0; k < 1 + kMaxStr; k++) {
-            unsigned long long x = val[k];
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const unsigned long long o = __shfl_up_sync(0xffffffffu, x, d);
-                if (lane >= d) x += o;
-            }
-            const unsigned long long ex = carry[k] + x - val[k];
-            carry[k] += __shfl_sync(0xffffffffu, x, 31);
-            if (i < hi) {
-                if (k == 0) sums[i].rows = (uint32_t)ex;
-                else sums[i].arena[k - 1] = (uint32_t)ex;
-            }
-        }
-    }
-}
-
-}  // namespace falx

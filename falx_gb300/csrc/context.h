@@ -54,8 +54,9 @@ struct falx_ctx {
     uint64_t tape_seps_cap = 0;     // bytes
     uint64_t *tape_ends = nullptr;
     uint64_t tape_ends_cap = 0;     // bytes
-    void *rec_sums = nullptr;
+    void *rec_sums = nullptr;       // look-back records of the columns pass
     uint64_t rec_sums_cap = 0;      // bytes
+    uint32_t col_epoch = 0;         // their tag
     // per-launch timing of the last rows call (FALX_OPT_TIMING)
     int timing = 0;
     cudaEvent_t ev[5] = {};

@@ -339,7 +339,7 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
 }
 
 template <int D, bool SPEC = false>
-__global__ void __launch_bounds__(kThreads) index_kernel(const __grid_constant__ Params p) {
+__global__ void __launch_bounds__(kThreads, 3) index_kernel(const __grid_constant__ Params p) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     SmemIx &S = *reinterpret_cast<SmemIx *>(smem_raw);
     const int tid = threadIdx.x;
@@ -773,23 +773,24 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     cp.hdr = c->hdr;
     cp.rows = rs;
     const uint64_t blocks = (cp.n_recs + kRecBlock - 1) / kRecBlock;
-    rc = grow_scratch(&c->rec_sums, &c->rec_sums_cap, blocks * sizeof(RecSums));
-    if (rc) return rc;
-    cp.sums = static_cast<RecSums *>(c->rec_sums);
-    // count rows and string bytes per block, scan, then decode
-    const size_t smem_cells = sizeof(ColSmem), smem_count = offsetof(ColSmem, data);
+    // look-back records, tagged with a per-call epoch: cleared only when
+    // (re)allocated and when the epoch wraps
+    if (blocks * sizeof(BlkStatus) > c->rec_sums_cap || c->col_epoch >= (1u << 29)) {
+        rc = grow_scratch(&c->rec_sums, &c->rec_sums_cap, blocks * sizeof(BlkStatus));
+        if (rc) return rc;
+        FALX_CUDA(cudaMemsetAsync(c->rec_sums, 0, c->rec_sums_cap, c->stream));
+        c->col_epoch = 0;
+    }
+    cp.status = static_cast<BlkStatus *>(c->rec_sums);
+    cp.epoch = ++c->col_epoch;
+    cp.n_blocks = (uint32_t)blocks;
+    const size_t smem_cells = sizeof(ColSmem);
 #define FALX_COLS(D)                                                                                           \
     do {                                                                                                       \
-        FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D, false>,                                 \
+        FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D>,                                        \
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cells));         \
-        FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D, true>,                                  \
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_count));         \
-        columns_kernel<D, true><<<(unsigned)blocks, kThreads, smem_count, c->stream>>>(cp);                    \
+        columns_kernel<D><<<(unsigned)blocks, kThreads, smem_cells, c->stream>>>(cp);                          \
         if (c->timing) cudaEventRecord(c->ev[2], c->stream);                                                   \
-        columns_scan<<<1, 1024, 0, c->stream>>>(cp.sums, (uint32_t)blocks, c->hdr);                            \
-        if (c->timing) cudaEventRecord(c->ev[3], c->stream);                                                   \
-        columns_kernel<D, false><<<(unsigned)blocks, kThreads, smem_cells, c->stream>>>(cp);                   \
-        if (c->timing) cudaEventRecord(c->ev[4], c->stream);                                                   \
     } while (0)
     switch (dialect) {
     case FALX_CSV: FALX_COLS(D_CSV); break;
@@ -802,8 +803,8 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
     FALX_CUDA(cudaStreamSynchronize(c->stream));
     if (c->timing) {
-        for (int k = 0; k < 4; k++) cudaEventElapsedTime(&c->last_ms[k], c->ev[k], c->ev[k + 1]);
-        c->last_n = 4;
+        for (int k = 0; k < 2; k++) cudaEventElapsedTime(&c->last_ms[k], c->ev[k], c->ev[k + 1]);
+        c->last_n = 2;
     }
     if (c->hhdr->error & (ERR_TIMEOUT | ERR_TMA)) return FALX_ERR_TIMEOUT;
     for (int k = 0; k < kMaxStr; k++)

@@ -69,8 +69,8 @@ void falx_destroy(falx_ctx *ctx);
 #define FALX_OPT_TIMING 3 /* 1: time each launch of the rows path with CUDA events */
 int falx_set_option(falx_ctx *ctx, int option, int value);
 /* Device times (ms) of the last rows call's launches, in order: index + tape,
- * row / string-byte count, block scan, cells. Returns how many were recorded
- * (0 unless FALX_OPT_TIMING is on and the default rows path ran). */
+ * columns. Returns how many were recorded (0 unless FALX_OPT_TIMING is on
+ * and the default rows path ran). */
 int falx_last_timings(const falx_ctx *ctx, float *ms, int n);
 /* Use `stream` (a cudaStream_t; NULL = the legacy default stream). */
 int falx_set_stream(falx_ctx *ctx, void *stream);
