@@ -69,10 +69,6 @@ struct ColSmem {
     uint32_t warp_len[kWarps][kMaxStr];
     uint32_t row_base;
     uint32_t arena_base[kMaxStr];
-    uint64_t sep_lo;
-    uint32_t sep_n;
-    int64_t data_lo;  // file position of data[0]
-    uint32_t data_n;
     uint64_t vbits[kMaxCols][kRecWords];
     unsigned long long red[kWarps][12];
     alignas(16) uint8_t data[kDataWin + 16];  // 16 bytes of slack for word reads near the window end
@@ -302,6 +298,37 @@ __device__ __forceinline__ uint32_t record_field_bytes(const Win &W, const Rec &
     return tot;
 }
 
+// Record li of the block starting at record R0 (E[li] = ends[R0 + li - 1]).
+template <int D>
+__device__ __forceinline__ Rec make_rec(const ColParams &p, const Win &W, const uint64_t *E, uint64_t R0, int li) {
+    Rec x;
+    x.row = false;
+    x.nf = 0;
+    x.start = x.end = x.end2 = x.sb = 0;
+    const uint64_t r = R0 + (uint64_t)li;
+    if (r >= p.n_recs) return x;
+    const uint64_t pe = r == 0 ? 0ull : E[li];
+    x.start = r == 0 ? 0u : (uint32_t)pe + 1;
+    x.sb = r == 0 ? 0u : (uint32_t)(pe >> 32);
+    // after the last terminator there is a record only if bytes remain
+    // (csv_geo.rs:1094-1100)
+    if (r >= p.n_ends && (uint64_t)x.start >= p.len) return x;
+    uint32_t se;
+    if (r < p.n_ends) {
+        const uint64_t e = E[li + 1];
+        x.end = (uint32_t)e;
+        se = (uint32_t)(e >> 32);
+    } else {
+        x.end = (uint32_t)p.len;
+        se = (uint32_t)p.n_seps;
+    }
+    x.nf = se - x.sb + 1;
+    x.row = !(D == D_CSV_HASH && x.start < x.end && W.byte(x.start) == '#');
+    x.end2 = x.end;
+    if (x.row && x.end > x.start && W.byte(x.end - 1) == '\r') x.end2 = x.end - 1;
+    return x;
+}
+
 template <int D>
 __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_constant__ ColParams p) {
     extern __shared__ __align__(16) uint8_t col_smem_raw[];
@@ -312,9 +339,32 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
     const uint64_t R0 = (uint64_t)blk * kRecBlock;
     for (int i = tid; i < rs.ncols * kRecWords; i += kThreads) S.vbits[i / kRecWords][i % kRecWords] = 0;
 
-    // ---- stage the tape entries of the block's records: ends[R0 - 1 ..
-    // R0 + kRecBlock - 1] in 16-byte pairs from the even index R0 - 2
+    // ---- windows: from the block's first record to its last, computed by
+    // every thread from the two tape entries that bound them
+    const uint64_t last = (R0 + kRecBlock < p.n_recs ? R0 + kRecBlock : p.n_recs) - 1;
+    const uint64_t e_first = R0 == 0 ? 0ull : __ldg(reinterpret_cast<const unsigned long long *>(p.ends) + R0 - 1);
+    const uint64_t e_last = last < p.n_ends ? __ldg(reinterpret_cast<const unsigned long long *>(p.ends) + last) : 0ull;
     const bool al16 = ((uintptr_t)p.ends & 15) == 0 && ((uintptr_t)p.seps & 15) == 0;
+    const uint64_t sb = R0 == 0 ? 0 : e_first >> 32;
+    const uint64_t se = last < p.n_ends ? e_last >> 32 : p.n_seps;
+    const uint64_t sep_lo = al16 ? sb & ~3ull : sb;  // 16-byte aligned start
+    const uint32_t sep_n = (uint32_t)(sb - sep_lo) + (uint32_t)(se - sb < (uint64_t)kSepWin ? se - sb : (uint64_t)kSepWin);
+    int64_t data_lo;
+    uint32_t data_n;
+    {
+        const int64_t lo = R0 == 0 ? 0 : (int64_t)(uint32_t)e_first + 1;
+        const int64_t hi = last < p.n_ends ? (int64_t)(uint32_t)e_last : (int64_t)p.len;
+        const int64_t q0 = (lo + p.shift) & ~15ll;  // 16-byte aligned address offset
+        const int64_t qend = (int64_t)((p.shift + p.len + 15) & ~15ull);
+        int64_t qn = ((hi + p.shift + 15) & ~15ll) - q0;
+        if (qn > qend - q0) qn = qend - q0;
+        if (qn > kDataWin) qn = kDataWin;
+        if (qn < 0) qn = 0;
+        data_lo = q0 - p.shift;
+        data_n = (uint32_t)qn;
+    }
+    // ---- stage the block's tape entries (ends[R0 - 1 .. R0 + kRecBlock - 1]
+    // in 16-byte pairs from the even index R0 - 2), separators and bytes
     for (int j = tid; j < (kRecBlock + 2) / 2; j += kThreads) {
         const int64_t e0 = (int64_t)R0 - 2 + 2 * j;
         if (al16 && e0 >= 0 && (uint64_t)e0 + 1 < p.n_ends) {
@@ -324,52 +374,26 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
             if (e0 + 1 >= 0 && (uint64_t)(e0 + 1) < p.n_ends) cp_async_ca<8>(&S.ends[2 * j + 1], p.ends + e0 + 1);
         }
     }
+    if (al16) {
+        for (uint32_t j = tid; 4 * j < sep_n; j += kThreads) {
+            const uint64_t i0 = sep_lo + 4 * j;
+            if (i0 + 3 < p.n_seps) {
+                cp_async_ca<16>(&S.seps[4 * j], p.seps + i0);
+            } else {
+                for (uint32_t q = 0; q < 4 && i0 + q < p.n_seps; q++) cp_async_ca<4>(&S.seps[4 * j + q], p.seps + i0 + q);
+            }
+        }
+    } else {
+        for (uint32_t i = tid; i < sep_n; i += kThreads) cp_async_ca<4>(&S.seps[i], p.seps + sep_lo + i);
+    }
+    {
+        const uint8_t *src = p.abase + (data_lo + p.shift);
+        for (uint32_t i = tid; i < data_n / 16; i += kThreads) cp_async_ca<16>(S.data + 16 * i, src + 16 * i);
+    }
     cp_async_wait_all();
     __syncthreads();
     const uint64_t *E = S.ends + 1;  // E[i] = ends[R0 - 1 + i]
-    if (tid == 0) {
-        // separator and byte windows: from the block's first record to its last
-        const uint64_t last = (R0 + kRecBlock < p.n_recs ? R0 + kRecBlock : p.n_recs) - 1;
-        const uint64_t sb = R0 == 0 ? 0 : E[0] >> 32;
-        const uint64_t se = last < p.n_ends ? E[last - R0 + 1] >> 32 : p.n_seps;
-        const uint64_t sb4 = al16 ? sb & ~3ull : sb;  // 16-byte aligned start
-        S.sep_lo = sb4;
-        S.sep_n = (uint32_t)(sb - sb4) + (uint32_t)(se - sb < (uint64_t)kSepWin ? se - sb : (uint64_t)kSepWin);
-        const int64_t lo = R0 == 0 ? 0 : (int64_t)(uint32_t)E[0] + 1;
-        const int64_t hi = last < p.n_ends ? (int64_t)(uint32_t)E[last - R0 + 1] : (int64_t)p.len;
-        const int64_t q0 = (lo + p.shift) & ~15ll;  // 16-byte aligned address offset
-        const int64_t qend = (int64_t)((p.shift + p.len + 15) & ~15ull);
-        int64_t qn = ((hi + p.shift + 15) & ~15ll) - q0;
-        if (qn > qend - q0) qn = qend - q0;
-        if (qn > kDataWin) qn = kDataWin;
-        if (qn < 0) qn = 0;
-        S.data_lo = q0 - p.shift;
-        S.data_n = (uint32_t)qn;
-    }
-    __syncthreads();
-    {
-        const uint32_t sn = S.sep_n;
-        const uint64_t sl = S.sep_lo;
-        if (al16) {
-            for (uint32_t j = tid; 4 * j < sn; j += kThreads) {
-                const uint64_t i0 = sl + 4 * j;
-                if (i0 + 3 < p.n_seps) {
-                    cp_async_ca<16>(&S.seps[4 * j], p.seps + i0);
-                } else {
-                    for (uint32_t q = 0; q < 4 && i0 + q < p.n_seps; q++) cp_async_ca<4>(&S.seps[4 * j + q], p.seps + i0 + q);
-                }
-            }
-        } else {
-            for (uint32_t i = tid; i < sn; i += kThreads) cp_async_ca<4>(&S.seps[i], p.seps + sl + i);
-        }
-    }
-    {
-        const uint8_t *src = p.abase + (S.data_lo + p.shift);
-        for (uint32_t i = tid; i < S.data_n / 16; i += kThreads) cp_async_ca<16>(S.data + 16 * i, src + 16 * i);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    const Win W{S.seps, S.data, p.seps, p.data, (uint32_t)S.sep_lo, S.sep_n, (uint32_t)S.data_lo, S.data_n};
+    const Win W{S.seps, S.data, p.seps, p.data, (uint32_t)sep_lo, sep_n, (uint32_t)data_lo, data_n};
 
     // ---- this thread's records: warp w owns records [64 w, 64 w + 64) of
     // the block and lane L takes records L and L + 32 of them, so a warp's
@@ -377,34 +401,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
     // records
     Rec rec[kRecPerThread];
 #pragma unroll
-    for (int i = 0; i < kRecPerThread; i++) {
-        const int li = warp * 64 + i * 32 + lane;  // E[li] = ends[r - 1]
-        const uint64_t r = R0 + (uint64_t)li;
-        Rec &x = rec[i];
-        x.row = false;
-        x.nf = 0;
-        x.start = x.end = x.end2 = x.sb = 0;
-        if (r >= p.n_recs) continue;
-        const uint64_t pe = r == 0 ? 0ull : E[li];
-        x.start = r == 0 ? 0u : (uint32_t)pe + 1;
-        x.sb = r == 0 ? 0u : (uint32_t)(pe >> 32);
-        // after the last terminator there is a record only if bytes remain
-        // (csv_geo.rs:1094-1100)
-        if (r >= p.n_ends && (uint64_t)x.start >= p.len) continue;
-        uint32_t se;
-        if (r < p.n_ends) {
-            const uint64_t e = E[li + 1];
-            x.end = (uint32_t)e;
-            se = (uint32_t)(e >> 32);
-        } else {
-            x.end = (uint32_t)p.len;
-            se = (uint32_t)p.n_seps;
-        }
-        x.nf = se - x.sb + 1;
-        x.row = !(D == D_CSV_HASH && x.start < x.end && W.byte(x.start) == '#');
-        x.end2 = x.end;
-        if (x.row && x.end > x.start && W.byte(x.end - 1) == '\r') x.end2 = x.end - 1;
-    }
+    for (int i = 0; i < kRecPerThread; i++) rec[i] = make_rec<D>(p, W, E, R0, warp * 64 + i * 32 + lane);
 
     // ---- per record: row (0/1) and cleaned bytes of each string slot
     const int nv = 1 + rs.nstr;  // values scanned: rows, then string slots
@@ -541,10 +538,60 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
                 for (int k = 0; k < kMaxStr; k++) p.hdr->arena[k] = pre[1 + k] + tot[1 + k];
             }
         }
+        if (lane == 0)
+            for (int k = 0; k < 11; k++) S.red[0][k] = 0;
+    } else {
+        // ---- meanwhile warps 1-7: field-byte and count / sum totals of all
+        // the block's records (they need no prefix), warp sums into shared
+        // memory for the block totals at the end
+        StatAcc acc = {};
+        uint32_t fb_fields = 0, fb_bytes = 0;  // below 2^32: the input is shorter than 4 GiB
+        if (rs.want_fb || rs.want_stats) {
+            for (int li = tid - 32; li < kRecBlock; li += kThreads - 32) {
+                const Rec x = make_rec<D>(p, W, E, R0, li);
+                if (!x.row) continue;
+                if (rs.want_stats) {
+                    acc.records++;
+#pragma unroll
+                    for (int k = 0; k < 2; k++) {
+                        uint32_t a, b;
+                        if (W.field(x, rs.stats_field[k], a, b)) stat_value(acc, k, W, a, b);
+                    }
+                }
+                if (rs.want_fb) {
+                    fb_fields += x.nf;
+                    fb_bytes += record_field_bytes(W, x);
+                }
+            }
+        }
+        unsigned long long r[11] = {fb_fields, fb_bytes, acc.records, acc.values[0], acc.values[1], acc.checksum[0],
+                                    acc.checksum[1], acc.sum_e6[0], acc.sum_e6[1], acc.inexact[0], acc.inexact[1]};
+        if (!rs.want_stats) {
+            uint32_t f = fb_fields, by = fb_bytes;
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+                f += __shfl_down_sync(0xffffffffu, f, d);
+                by += __shfl_down_sync(0xffffffffu, by, d);
+            }
+            r[0] = f;
+            r[1] = by;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 11; k++) {
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) r[k] += __shfl_down_sync(0xffffffffu, r[k], d);
+            }
+        }
+        if (lane == 0)
+            for (int k = 0; k < 11; k++) S.red[warp][k] = r[k];
     }
     __syncthreads();
+    const int nred = rs.want_stats ? 11 : rs.want_fb ? 2 : 0;
 
-    // ---- cells, column by column
+    // ---- cells, column by column (the records are read again from shared
+    // memory: cheaper than keeping them in registers across the look-back)
+#pragma unroll
+    for (int i = 0; i < kRecPerThread; i++) rec[i] = make_rec<D>(p, W, E, R0, warp * 64 + i * 32 + lane);
     const uint32_t row_base = S.row_base;
     const uint32_t wrow = S.warp_rows[warp];  // the warp's first row, block-relative
     uint32_t grow[kRecPerThread];             // file row of each record
@@ -628,52 +675,6 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
             else okm[0] |= (uint32_t)ok << c;
         }
     }
-    StatAcc acc = {};
-    uint32_t fb_fields = 0, fb_bytes = 0;  // below 2^32: the input is shorter than 4 GiB
-#pragma unroll 1
-    for (int i = 0; i < kRecPerThread; i++) {
-        const Rec x = i ? rec[1] : rec[0];
-        if (!x.row) continue;
-        if (rs.want_stats) {
-            acc.records++;
-#pragma unroll
-            for (int k = 0; k < 2; k++) {
-                uint32_t a, b;
-                if (W.field(x, rs.stats_field[k], a, b)) stat_value(acc, k, W, a, b);
-            }
-        }
-        if (rs.want_fb) {
-            fb_fields += x.nf;
-            fb_bytes += record_field_bytes(W, x);
-        }
-    }
-
-    // ---- field-byte and count / sum totals: warp sums into shared memory
-    // (read after the barrier below), one global atomic per value and block
-    const int nred = rs.want_stats ? 11 : rs.want_fb ? 2 : 0;
-    if (nred) {
-        unsigned long long r[11] = {fb_fields, fb_bytes, acc.records, acc.values[0], acc.values[1], acc.checksum[0],
-                                    acc.checksum[1], acc.sum_e6[0], acc.sum_e6[1], acc.inexact[0], acc.inexact[1]};
-        if (nred == 2) {
-            uint32_t f = fb_fields, by = fb_bytes;
-#pragma unroll
-            for (int d = 16; d > 0; d >>= 1) {
-                f += __shfl_down_sync(0xffffffffu, f, d);
-                by += __shfl_down_sync(0xffffffffu, by, d);
-            }
-            r[0] = f;
-            r[1] = by;
-        } else {
-#pragma unroll
-            for (int k = 0; k < 11; k++) {
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) r[k] += __shfl_down_sync(0xffffffffu, r[k], d);
-            }
-        }
-        if (lane == 0)
-            for (int k = 0; k < nred; k++) S.red[warp][k] = r[k];
-    }
-
     // ---- validity: the warp's rows are consecutive, at most 64 of them;
     // one 64-bit word per column and warp. With every record a row, record
     // L + 32 i of the warp is its row L + 32 i and the word is two ballots;
