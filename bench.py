@@ -272,21 +272,26 @@ def bench_gpu(args):
             ent["dram_gbs"] = round(traffic_per[name] / (kt / 1e3) / 1e9, 1)
         kernels.append(ent)
 
-    # End to end through the host-buffer C ABI entry point.
-    h_index = np.empty(idx_cap, dtype=np.uint32)
+    # End to end through the host-buffer C ABI entry point; input and output
+    # buffers in pinned host memory.
+    def pinned_np(count, dtype):
+        t = torch.empty(count * np.dtype(dtype).itemsize, dtype=torch.uint8, pin_memory=True)
+        return t.numpy().view(dtype)
+
+    h_index = pinned_np(idx_cap, np.uint32)
     h_vals = []
     hcols = _lib.falx_columns()
     hcols.rows_cap = rows_cap
     for k, (f, t) in enumerate(SCHEMA_COLS):
         if t == fx.STR:
-            v = np.empty(rows_cap + 1, dtype=np.int32)
-            sd = np.empty(str_cap, dtype=np.uint8)
+            v = pinned_np(rows_cap + 1, np.int32)
+            sd = pinned_np(str_cap, np.uint8)
             hcols.cols[k].str_data = sd.ctypes.data
             hcols.cols[k].str_cap = str_cap
         else:
-            v = np.empty(rows_cap, dtype=np.float64 if t == fx.F64 else np.uint32)
+            v = pinned_np(rows_cap, np.float64 if t == fx.F64 else np.uint32)
             sd = None
-        valid = np.empty((rows_cap + 63) // 64, dtype=np.uint64)
+        valid = pinned_np((rows_cap + 63) // 64, np.uint64)
         hcols.cols[k].values = v.ctypes.data
         hcols.cols[k].valid = valid.ctypes.data
         h_vals.append((v, valid, sd))

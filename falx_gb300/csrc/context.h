@@ -54,6 +54,12 @@ struct falx_ctx {
     uint64_t tape_seps_cap = 0;     // bytes
     uint64_t *tape_ends = nullptr;
     uint64_t tape_ends_cap = 0;     // bytes
+    // host-buffer parse: the structural index is copied back on its own
+    // stream while the columns kernel runs
+    cudaStream_t copy_stream = nullptr;
+    uint32_t *host_index = nullptr;
+    uint64_t host_index_cap = 0;
+    bool host_index_done = false;
     void *rec_sums = nullptr;       // look-back records of the columns pass
     uint64_t rec_sums_cap = 0;      // bytes
     uint32_t col_epoch = 0;         // their tag

@@ -759,6 +759,13 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
         if (rc) return rc;
     }
     if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    if (c->host_index && P.index) {
+        // the index is final (the host has waited for the index kernel):
+        // copy it back while the columns kernel runs
+        const uint64_t ni = n_struct < c->host_index_cap ? n_struct : c->host_index_cap;
+        if (ni) FALX_CUDA(cudaMemcpyAsync(c->host_index, P.index, ni * 4, cudaMemcpyDeviceToHost, c->copy_stream));
+        c->host_index_done = true;
+    }
     ColParams cp;
     memset(&cp, 0, sizeof cp);
     cp.data = data;
@@ -969,6 +976,7 @@ void falx_destroy(falx_ctx *c) {
     if (c->tape_seps) cudaFree(c->tape_seps);
     if (c->tape_ends) cudaFree(c->tape_ends);
     if (c->rec_sums) cudaFree(c->rec_sums);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     for (int k = 0; k < 5; k++)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
     delete c;
@@ -1168,7 +1176,17 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
         }
         d.columns = &dc;
     }
+    if (host_out->index_cap && host_out->index && hc) {
+        if (!c->copy_stream) FALX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        c->host_index = host_out->index;
+        c->host_index_cap = host_out->index_cap;
+        c->host_index_done = false;
+    }
     rc = parse_device(c, schema, c->dev_in, len, &d);
+    const bool index_done = c->host_index_done;
+    c->host_index = nullptr;
+    c->host_index_done = false;
+    if (index_done) FALX_CUDA(cudaStreamSynchronize(c->copy_stream));
     if (rc && rc != FALX_ERR_CAPACITY) return rc;
     auto back = [&](void *dst, const void *src, uint64_t bytes) -> int {
         if (bytes && dst) FALX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
@@ -1178,7 +1196,7 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     uint64_t ni = d.n_index < host_out->index_cap ? d.n_index : host_out->index_cap;
     uint64_t ns = d.n_seps < host_out->seps_cap ? d.n_seps : host_out->seps_cap;
     uint64_t ne = d.n_ends < host_out->ends_cap ? d.n_ends : host_out->ends_cap;
-    if (!r2) r2 = back(host_out->index, d.index, ni * 4);
+    if (!r2 && !index_done) r2 = back(host_out->index, d.index, ni * 4);
     if (!r2) r2 = back(host_out->seps, d.seps, ns * 4);
     if (!r2) r2 = back(host_out->ends, d.ends, ne * 8);
     if (hc) {
