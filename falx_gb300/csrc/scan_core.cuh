@@ -257,9 +257,16 @@ __device__ __forceinline__ uint64_t structural_mask(const Masks &m, uint64_t ls_
             return m.s & ~((1ull << (__ffsll((long long)m.nl) - 1)) - 1);
         }
         uint64_t h = m.x & ls_bits;
-        if (h == 0 && state != R_C) {
-            uint64_t inq = prefix_xor64(m.q) ^ (state == R_Q ? ~0ull : 0ull);
-            return m.s & ~inq;
+        if (h == 0) {
+            const uint64_t inq = prefix_xor64(m.q);
+            if (state != R_C) return m.s & ~(inq ^ (state == R_Q ? ~0ull : 0ull));
+            // a comment runs to the first newline; from there the state is
+            // NORMAL and quote parity restarts: inside quotes where the prefix
+            // XOR differs from its value just before the newline
+            if (m.nl == 0) return 0;
+            const uint64_t from = ~0ull << (__ffsll((long long)m.nl) - 1);
+            const uint64_t before = (uint64_t)(__popcll(m.q & ~from) & 1);
+            return m.s & from & ~(inq ^ (0ull - before));
         }
         uint32_t s = state;
         uint64_t inert = resolve_regions(m.q, h, m.nl, s);

@@ -324,6 +324,9 @@ __device__ void lookback_cta(const Params &p, LookbackSmem &L, uint32_t tile, ui
         }
         uint32_t f = kIdentity;
         uint64_t c[4] = {0, 0, 0, 0};
+        // warps whose predecessors all lie at or past the inclusive prefix
+        // contribute nothing: they skip the fold (warp-uniform)
+        const bool active = (uint32_t)(warp * 32) < sidx;
         if (in && (uint32_t)tid < sidx) {
             if (!SPEC) {
                 f = ld_relaxed(&p.status[j].func);
@@ -347,18 +350,20 @@ __device__ void lookback_cta(const Params &p, LookbackSmem &L, uint32_t tile, ui
                 }
             }
         }
+        if (active) {
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t gf = __shfl_down_sync(0xffffffffu, f, d);
-            uint64_t gc[4];
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t gf = __shfl_down_sync(0xffffffffu, f, d);
+                uint64_t gc[4];
 #pragma unroll
-            for (int s0 = 0; s0 < NS; s0++) gc[s0] = __shfl_down_sync(0xffffffffu, c[s0], d);
-            if (lane + d < 32) {
-                if (SPEC) agg_prepend_spec<NS>(gf, gc, f, c);
-                else agg_prepend<NS>(gf, gc, f, c);
+                for (int s0 = 0; s0 < NS; s0++) gc[s0] = __shfl_down_sync(0xffffffffu, c[s0], d);
+                if (lane + d < 32) {
+                    if (SPEC) agg_prepend_spec<NS>(gf, gc, f, c);
+                    else agg_prepend<NS>(gf, gc, f, c);
+                }
             }
         }
-        if (lane == 0) {
+        if (lane == 0 && active) {
             L.wf[warp] = f;
 #pragma unroll
             for (int s0 = 0; s0 < NS; s0++) L.wc[warp][s0] = c[s0];
@@ -371,7 +376,8 @@ __device__ void lookback_cta(const Params &p, LookbackSmem &L, uint32_t tile, ui
         }
         __syncthreads();
         if (tid == 0) {
-            for (int w = 0; w < kWarps; w++) {
+            const int nw = sidx >= (uint32_t)kThreads ? kWarps : (int)((sidx + 31) / 32);
+            for (int w = 0; w < nw; w++) {
                 unsigned long long g[4];
 #pragma unroll
                 for (int s0 = 0; s0 < NS; s0++) g[s0] = L.wc[w][s0];
