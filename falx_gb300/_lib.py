@@ -88,6 +88,8 @@ SIGNATURES = {
     "falx_set_stream": (c_int, [c_void_p, c_void_p]),
     "falx_set_option": (c_int, [c_void_p, c_int, c_int]),
     "falx_last_timings": (c_int, [c_void_p, POINTER(c_float), c_int]),
+    "falx_test_stalled_lookback": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, POINTER(falx_columns),
+                                           c_uint64]),
     "falx_strerror": (c_char_p, [c_int]),
     "falx_index_structurals": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64)]),
     "falx_parse_tape": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64, c_void_p, c_uint64,

@@ -55,6 +55,8 @@ struct ColParams {
     BlkStatus *status;  // per record block
     uint32_t epoch;
     uint32_t n_blocks;
+    uint32_t blk0;     // first record block of the launch (block b runs as blk0 + b)
+    uint64_t wait_ns;  // look-back wait limit
     DevHeader *hdr;
     RowSpec rows;
 };
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
     ColSmem &S = *reinterpret_cast<ColSmem *>(col_smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const RowSpec &rs = p.rows;
-    const uint32_t blk = blockIdx.x;
+    const uint32_t blk = p.blk0 + blockIdx.x;
     const uint64_t R0 = (uint64_t)blk * kRecBlock;
     for (int i = tid; i < rs.ncols * kRecWords; i += kThreads) S.vbits[i / kRecWords][i % kRecWords] = 0;
 
@@ -495,7 +497,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
                 const uint32_t fm = bm ? __ffs(bm) - 1 : 32u;
                 if (fm > fi || bm == 0) break;
                 if ((it & 15) == 15) {
-                    const bool stop = lane == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > kWaitNs);
+                    const bool stop = lane == 0 && (aborted(p.hdr) || globaltimer_ns() - t0 > p.wait_ns);
                     if (__any_sync(0xffffffffu, stop)) {
                         if (lane == 0) fail(p.hdr, ERR_TIMEOUT);
                         fi = 0;

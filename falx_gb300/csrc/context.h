@@ -63,6 +63,7 @@ struct falx_ctx {
     void *rec_sums = nullptr;       // look-back records of the columns pass
     uint64_t rec_sums_cap = 0;      // bytes
     uint32_t col_epoch = 0;         // their tag
+    uint64_t stall_test_ns = 0;     // falx_test_stalled_lookback
     // per-launch timing of the last rows call (FALX_OPT_TIMING)
     int timing = 0;
     cudaEvent_t ev[5] = {};

@@ -791,12 +791,21 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     cp.status = static_cast<BlkStatus *>(c->rec_sums);
     cp.epoch = ++c->col_epoch;
     cp.n_blocks = (uint32_t)blocks;
+    cp.wait_ns = kWaitNs;
+    uint64_t grid = blocks;
+    if (c->stall_test_ns) {
+        // test hook: run record block 1 alone, so its look-back waits for a
+        // block 0 that never publishes and gives up after the given limit
+        cp.blk0 = 1;
+        cp.wait_ns = c->stall_test_ns;
+        grid = blocks > 1 ? 1 : 0;
+    }
     const size_t smem_cells = sizeof(ColSmem);
 #define FALX_COLS(D)                                                                                           \
     do {                                                                                                       \
         FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D>,                                        \
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cells));         \
-        columns_kernel<D><<<(unsigned)blocks, kThreads, smem_cells, c->stream>>>(cp);                          \
+        if (grid) columns_kernel<D><<<(unsigned)grid, kThreads, smem_cells, c->stream>>>(cp);                  \
         if (c->timing) cudaEventRecord(c->ev[2], c->stream);                                                   \
     } while (0)
     switch (dialect) {
@@ -1001,6 +1010,15 @@ int falx_set_option(falx_ctx *c, int option, int value) {
     default:
         return FALX_ERR_INVALID;
     }
+}
+
+int falx_test_stalled_lookback(falx_ctx *c, const falx_schema *schema, const uint8_t *data, uint64_t len,
+                                falx_columns *out, uint64_t wait_ns) {
+    if (!c || !schema || !out || !wait_ns) return FALX_ERR_INVALID;
+    c->stall_test_ns = wait_ns;
+    const int rc = falx_parse_columns(c, schema, data, len, out);
+    c->stall_test_ns = 0;
+    return rc;
 }
 
 int falx_last_timings(const falx_ctx *c, float *ms, int n) {

@@ -72,6 +72,7 @@ int falx_set_option(falx_ctx *ctx, int option, int value);
  * columns. Returns how many were recorded (0 unless FALX_OPT_TIMING is on
  * and the default rows path ran). */
 int falx_last_timings(const falx_ctx *ctx, float *ms, int n);
+
 /* Use `stream` (a cudaStream_t; NULL = the legacy default stream). */
 int falx_set_stream(falx_ctx *ctx, void *stream);
 const char *falx_strerror(int code);
@@ -123,6 +124,14 @@ typedef struct {
  * (csv_hash) are not rows. */
 int falx_parse_columns(falx_ctx *ctx, const falx_schema *schema, const uint8_t *data, uint64_t len,
                        falx_columns *out);
+
+/* Test hook for failure detection (no reference counterpart): as
+ * falx_parse_columns, but only record block 1 of the columns pass runs, so
+ * its look-back waits for a block 0 that never publishes; the wait gives up
+ * after wait_ns and the call returns FALX_ERR_TIMEOUT with the context still
+ * usable. The input must hold more than 512 records. Outputs are undefined. */
+int falx_test_stalled_lookback(falx_ctx *ctx, const falx_schema *schema, const uint8_t *data, uint64_t len,
+                               falx_columns *out, uint64_t wait_ns);
 
 typedef struct {
     uint64_t records;
