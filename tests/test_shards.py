@@ -94,3 +94,49 @@ def test_gloo_two_ranks(tmp_path):
     path = str(tmp_path / "result")
     mp.spawn(_rank, args=(2, port, path), nprocs=2, join=True)
     assert open(path).read() == "ok"
+
+
+def _rank_fails(rank, world, port, path):
+    import datetime
+
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=5))
+    if rank == 1:
+        os._exit(3)  # the rank dies before the summary exchange
+    doc = bytes(gen.generate(gen.CSV_HASH, 64 << 10))
+    lo, hi = shards.shard_bounds(len(doc), world)[rank]
+    try:
+        shards.parse_sharded(OracleShards(), doc[lo:hi], 1, rank, lo, -1, shards.torch_all_gather)
+        outcome = "no error"
+    except Exception as e:  # the exchange fails instead of hanging
+        outcome = "detected: " + type(e).__name__
+    with open(path, "w") as f:
+        f.write(outcome)
+    os._exit(0)
+
+
+def test_gloo_rank_failure_is_detected(tmp_path):
+    # A rank that dies before the exchange: the surviving rank's all-gather
+    # ends with an error (peer gone or the process-group timeout), never a
+    # hang, and no GPU work of it is in flight.
+    import time
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    path = str(tmp_path / "result")
+    ctx = mp.spawn(_rank_fails, args=(2, port, path), nprocs=2, join=False)
+    t0 = time.time()
+    for p in ctx.processes:
+        p.join(timeout=60)
+    alive = [p for p in ctx.processes if p.is_alive()]
+    for p in alive:
+        p.kill()
+    assert not alive, "a rank hung"
+    assert time.time() - t0 < 60
+    assert open(path).read().startswith("detected")
