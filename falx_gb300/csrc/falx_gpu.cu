@@ -64,14 +64,17 @@ struct SmemIx {
     uint32_t warp_f[kWarps];
     unsigned long long warp_agg[kWarps][4];
     unsigned long long warp_c[kWarps];
-    uint32_t tile_f, ptile_f;
-    unsigned long long agg[4], pagg[4];
+    // per-tile results of the local pass, two slots: the local pass of tile
+    // i writes slot i & 1 while the deferred output of tile i - 1 reads the
+    // other, so no hand-over copy (and no barrier pair) is needed
+    uint32_t tile_f[2];
+    unsigned long long agg[2][4];
     LookbackSmem lb;  // block-wide look-back
     uint32_t base[3];
     unsigned long long tile_c;
     // speculative index: entry state assumed by the tile in its local pass
     // and by the deferred one; counts of the look-back not known yet
-    uint32_t spec_p, pspec_p;
+    uint32_t spec_p[2];
 };
 
 // Local pass of one tile: classify, scan transfer functions, publish the
@@ -80,7 +83,8 @@ struct SmemIx {
 // file's initial state), counts only under that assumption and publishes
 // its full transfer function, the assumed entry and those counts.
 template <int D, bool SPEC, bool CROWS = false>
-__device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t tile, uint8_t *b, LocalState &L) {
+__device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t tile, uint8_t *b, LocalState &L,
+                                           int slot) {
     constexpr int kBuf = kPre + kTile;
     constexpr int NS = NStates<D>::value;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -122,7 +126,7 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
         uint32_t we = __shfl_up_sync(0xffffffffu, wi, 1);
         if (lane == 0) we = kIdentity;
         if (lane < kWarps) S.warp_f[lane] = we;
-        if (lane == kWarps - 1) S.tile_f = wi;
+        if (lane == kWarps - 1) S.tile_f[slot] = wi;
     }
     __syncthreads();
     L.excl = fcompose(S.warp_f[warp], excl);
@@ -150,11 +154,11 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
             TileStatus *tst = &p.status[tile];
             unsigned long long agg = 0;
             for (int w2 = 0; w2 < kWarps; w2++) agg += S.warp_agg[w2][0];
-            tst->func = S.tile_f | (pk << 8);
+            tst->func = S.tile_f[slot] | (pk << 8);
             tst->agg[0] = agg;
             st_release(&tst->flag, p.epoch * 4 + 1);
-            S.agg[0] = agg;
-            S.spec_p = pk;
+            S.agg[slot][0] = agg;
+            S.spec_p[slot] = pk;
         }
         return;
     }
@@ -182,12 +186,12 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
 #pragma unroll
         for (int s0 = 0; s0 < NS; s0++)
             for (int w2 = 0; w2 < kWarps; w2++) agg[s0] += S.warp_agg[w2][s0];
-        tst->func = SPEC ? (S.tile_f | (kAllStates << 8)) : S.tile_f;
+        tst->func = SPEC ? (S.tile_f[slot] | (kAllStates << 8)) : S.tile_f[slot];
 #pragma unroll
         for (int s0 = 0; s0 < NS; s0++) tst->agg[s0] = agg[s0];
         st_release(&tst->flag, p.epoch * 4 + 1);
-        for (int s0 = 0; s0 < 4; s0++) S.agg[s0] = agg[s0];
-        S.spec_p = kAllStates;
+        for (int s0 = 0; s0 < 4; s0++) S.agg[slot][s0] = agg[s0];
+        S.spec_p[slot] = kAllStates;
     }
 }
 
@@ -198,23 +202,24 @@ __device__ __forceinline__ void local_pass(const Params &p, SmemIx &S, uint32_t 
 // its true exit and counts at once (level 2), and then its inclusive prefix
 // when every count before it is known.
 template <int D, bool SPEC>
-__device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t tile, const LocalState &L) {
+__device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t tile, const LocalState &L,
+                                            int slot) {
     constexpr int NS = NStates<D>::value;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t vs = (int64_t)tile * kTile - (int64_t)p.shift;
     uint32_t entry, pre[3];
     bool unknown;
     lookback_cta<NS, SPEC>(p, S.lb, tile, entry, pre, unknown);
-    const bool full = !SPEC || S.pspec_p == kAllStates;  // counted under every entry
-    const bool hit = full || entry == S.pspec_p;         // block-uniform
+    const bool full = !SPEC || S.spec_p[slot] == kAllStates;  // counted under every entry
+    const bool hit = full || entry == S.spec_p[slot];         // block-uniform
     if (tid == 0 && hit && !unknown) {
         TileStatus *tst = &p.status[tile];
-        unsigned long long mine = S.pagg[0];
+        unsigned long long mine = S.agg[slot][0];
         if (full) {
 #pragma unroll
-            for (int t = 1; t < NS; t++) mine = entry == (uint32_t)t ? S.pagg[t] : mine;
+            for (int t = 1; t < NS; t++) mine = entry == (uint32_t)t ? S.agg[slot][t] : mine;
         }
-        tst->exit = fapply(S.ptile_f, entry);
+        tst->exit = fapply(S.tile_f[slot], entry);
         tst->incl[0] = pre[0] + cfield(mine, 0);
         tst->incl[1] = pre[1] + cfield(mine, 1);
         tst->incl[2] = pre[2] + cfield(mine, 2);
@@ -255,7 +260,7 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
         if (SPEC && !hit && lane == kWarps - 1) {
             // wrong assumption: true exit and recount for the successors
             TileStatus *tst = &p.status[tile];
-            tst->exit = fapply(S.ptile_f, entry);
+            tst->exit = fapply(S.tile_f[slot], entry);
             tst->agg[1] = wi;
             st_release(&tst->flag, p.epoch * 4 + 2);
             atomicAdd(&p.hdr->spec_repairs, 1ull);
@@ -278,7 +283,7 @@ __device__ __forceinline__ void output_pass(const Params &p, SmemIx &S, uint32_t
         if (tid == 0) {
             const unsigned long long mine = S.tile_c;
             TileStatus *tst = &p.status[tile];
-            if (hit) tst->exit = fapply(S.ptile_f, entry);
+            if (hit) tst->exit = fapply(S.tile_f[slot], entry);
             tst->incl[0] = pre[0] + cfield(mine, 0);
             tst->incl[1] = pre[1] + cfield(mine, 1);
             tst->incl[2] = pre[2] + cfield(mine, 2);
@@ -375,22 +380,15 @@ __global__ void __launch_bounds__(kThreads, 3) index_kernel(const __grid_constan
                 break;
             }
             phase[s] ^= 1;
-            local_pass<D, SPEC>(p, S, tile, S.buf[s], cur);
+            local_pass<D, SPEC>(p, S, tile, S.buf[s], cur, s);
             __syncthreads();  // buf[s] fully read
             if (tid == 0 && tile + 2 * G < p.num_tiles) {
                 fence_proxy_async();
                 issue_tile_ix(p, tile + 2 * G, S.buf[s], &S.bar[s]);
             }
         }
-        if (have_prev) output_pass<D, SPEC>(p, S, prev_tile, prev);
+        if (have_prev) output_pass<D, SPEC>(p, S, prev_tile, prev, s ^ 1);
         if (!has_cur) break;
-        __syncthreads();
-        if (tid == 0) {
-            S.ptile_f = S.tile_f;
-            for (int k = 0; k < 4; k++) S.pagg[k] = S.agg[k];
-            S.pspec_p = S.spec_p;
-        }
-        __syncthreads();
         prev = cur;
         prev_tile = tile;
         have_prev = true;
@@ -426,7 +424,7 @@ __global__ void __launch_bounds__(kThreads) summary_tiles_kernel(const __grid_co
             *reinterpret_cast<uint4 *>(dst + first + 16 * i) = reinterpret_cast<const uint4 *>(lo)[i];
         __syncthreads();
         LocalState L;
-        local_pass<D, false, true>(p, S, tile, S.buf[0], L);
+        local_pass<D, false, true>(p, S, tile, S.buf[0], L, 0);
         __syncthreads();
     }
 }
