@@ -60,6 +60,16 @@ struct falx_ctx {
     uint32_t *host_index = nullptr;
     uint64_t host_index_cap = 0;
     bool host_index_done = false;
+    // host-buffer parse: the input is copied in chunks on copy_stream, each
+    // followed by a flag write; the first index launch waits per tile for
+    // its chunk instead of for the whole copy
+    uint32_t *arrive = nullptr;      // device, kMaxArriveChunks flags
+    uint32_t arrive_tag = 0;
+    void *write_value = nullptr;     // cuStreamWriteValue32, from the driver
+    int write_value_state = 0;       // 0 not looked up, 1 available, -1 not
+    cudaEvent_t in_free = nullptr;   // earlier work on `stream` is done with the input buffer
+    const uint32_t *pend_arrive = nullptr;
+    uint32_t pend_tag = 0, pend_chunk_tiles = 0;
     void *rec_sums = nullptr;       // look-back records of the columns pass
     uint64_t rec_sums_cap = 0;      // bytes
     uint32_t col_epoch = 0;         // their tag

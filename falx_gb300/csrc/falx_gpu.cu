@@ -737,6 +737,12 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     }
     const RowSpec rs = P.rows;
     memset(&P.rows, 0, sizeof P.rows);
+    if (c->pend_arrive) {
+        P.arrive = c->pend_arrive;
+        P.arrive_tag = c->pend_tag;
+        P.chunk_tiles = c->pend_chunk_tiles;
+        c->pend_arrive = nullptr;
+    }
     c->last_n = 0;
     if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[0], c->stream));
     int rc = run_scan(c, dialect, false, data, len, P);
@@ -749,6 +755,7 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
         if (rc) return rc;
         P.index = nullptr;
         P.index_cap = 0;
+        P.arrive = nullptr;
         P.seps = c->tape_seps;
         P.seps_cap = c->tape_seps_cap / 4;
         P.ends = c->tape_ends;
@@ -984,6 +991,8 @@ void falx_destroy(falx_ctx *c) {
     if (c->tape_ends) cudaFree(c->tape_ends);
     if (c->rec_sums) cudaFree(c->rec_sums);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->arrive) cudaFree(c->arrive);
+    if (c->in_free) cudaEventDestroy(c->in_free);
     for (int k = 0; k < 5; k++)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
     delete c;
@@ -1144,6 +1153,66 @@ int falx_index_structurals_host(falx_ctx *c, int dialect, const uint8_t *host_da
 // Host-buffer form of falx_parse: `host_out` holds HOST pointers (index,
 // seps, ends, column buffers); they are staged through device buffers that
 // the context owns and reuses across calls.
+}  // extern "C"
+
+namespace {
+constexpr uint64_t kChunkedInMin = 64ull << 20;  // smaller inputs: one copy
+constexpr uint32_t kMaxArriveChunks = 64;
+constexpr uint32_t kArriveChunks = 8;
+typedef int (*WriteValue32Fn)(void *stream, unsigned long long addr, unsigned int value, unsigned int flags);
+
+// Copy host_data into c->dev_in as chunks on the copy stream, each followed
+// by a flag write (cuStreamWriteValue32: the driver fences the copy before
+// the write). Returns 1 when the chunks are queued and the first index
+// launch should wait on them, 0 when the caller should copy as usual.
+int start_chunked_input(falx_ctx *c, const uint8_t *host_data, uint64_t len) {
+    if (c->write_value_state == 0) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        c->write_value_state = -1;
+        if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess && fn) {
+            c->write_value = fn;
+            c->write_value_state = 1;
+        }
+        cudaGetLastError();
+    }
+    if (c->write_value_state != 1) return 0;
+    if (!c->copy_stream) FALX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    if (!c->in_free) FALX_CUDA(cudaEventCreateWithFlags(&c->in_free, cudaEventDisableTiming));
+    if (!c->arrive || c->arrive_tag >= 0x7FFFFFFFu) {
+        if (!c->arrive) FALX_CUDA(cudaMalloc(&c->arrive, kMaxArriveChunks * sizeof(uint32_t)));
+        FALX_CUDA(cudaMemsetAsync(c->arrive, 0, kMaxArriveChunks * sizeof(uint32_t), c->stream));
+        c->arrive_tag = 0;
+    }
+    const uint32_t tag = ++c->arrive_tag;
+    // the input buffer is overwritten only after earlier work on the stream
+    FALX_CUDA(cudaEventRecord(c->in_free, c->stream));
+    FALX_CUDA(cudaStreamWaitEvent(c->copy_stream, c->in_free, 0));
+    const uint64_t tiles = (len + kTile - 1) / kTile;  // dev_in is 256-byte aligned: no shift
+    const uint64_t ct = (tiles + kArriveChunks - 1) / kArriveChunks;
+    const WriteValue32Fn wv = (WriteValue32Fn)c->write_value;
+    for (uint32_t k = 0; k * ct < tiles; k++) {
+        const uint64_t lo = (uint64_t)k * ct * kTile, hi = std::min(len, (uint64_t)(k + 1) * ct * kTile);
+        FALX_CUDA(cudaMemcpyAsync(c->dev_in + lo, host_data + lo, hi - lo, cudaMemcpyHostToDevice, c->copy_stream));
+        if (wv((void *)c->copy_stream, (unsigned long long)(uintptr_t)(c->arrive + k), tag, 0) != 0) {
+            // no flag for this chunk: finish the copy before the kernel starts
+            FALX_CUDA(cudaMemcpyAsync(c->dev_in + hi, host_data + hi, len - hi, cudaMemcpyHostToDevice,
+                                      c->copy_stream));
+            FALX_CUDA(cudaStreamSynchronize(c->copy_stream));
+            c->write_value_state = -1;
+            return 0;
+        }
+    }
+    c->pend_arrive = c->arrive;
+    c->pend_tag = tag;
+    c->pend_chunk_tiles = (uint32_t)ct;
+    return 1;
+}
+}  // namespace
+
+extern "C" {
+
 int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_data, uint64_t len,
                     falx_outputs *host_out) {
     if (!c || !schema || !host_out || (len && !host_data)) return FALX_ERR_INVALID;
@@ -1177,7 +1246,16 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     rc = grow(&c->dev_out, &c->dev_out_cap, need);
     if (rc) return rc;
     uint8_t *dout = (uint8_t *)c->dev_out;
-    if (len) FALX_CUDA(cudaMemcpyAsync(c->dev_in, host_data, len, cudaMemcpyHostToDevice, c->stream));
+    // Large inputs on the default rows path: copy in chunks on the copy
+    // stream and let the index kernel start on the first chunk.
+    const bool rows_call = hc || host_out->field_bytes || host_out->stats;
+    bool chunked = false;
+    if (len >= kChunkedInMin && rows_call && c->rows_path == 0 && schema->dialect != FALX_NDJSON) {
+        rc = start_chunked_input(c, host_data, len);
+        if (rc < 0) return rc;
+        chunked = rc == 1;
+    }
+    if (len && !chunked) FALX_CUDA(cudaMemcpyAsync(c->dev_in, host_data, len, cudaMemcpyHostToDevice, c->stream));
     falx_outputs d = *host_out;
     falx_columns dc;
     if (host_out->index_cap) d.index = (uint32_t *)(dout + o_index);

@@ -79,6 +79,11 @@ struct Params {
     uint64_t sep_base;
     const uint8_t *pred;   // speculative index: assumed entry state of every tile
     uint8_t *states64;     // optional: entry state of every 64-byte block
+    // optional: input still arriving in chunks of chunk_tiles tiles; chunk k
+    // is in device memory once arrive[k] == arrive_tag
+    const uint32_t *arrive;
+    uint32_t arrive_tag;
+    uint32_t chunk_tiles;
     RowSpec rows;
 };
 
@@ -134,7 +139,22 @@ __device__ __forceinline__ void issue_tile(const Params &p, uint32_t t, uint8_t 
 }
 
 // Bulk copy of tile `t` (plus the kPre bytes before it) for the index kernel.
+// Input arriving in chunks (host-buffer calls): wait, bounded, until tile t's
+// chunk has landed. The flag is written by the copy stream after the chunk's
+// copy, behind a memory fence; chunks land in order, so the 16 bytes before
+// the tile (previous chunk) are there too.
+static __device__ __noinline__ bool wait_arrival(const Params &p, uint32_t t) {
+    const uint32_t k = t / p.chunk_tiles;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t i = 0;; i++) {
+        if (ld_acquire(p.arrive + k) == p.arrive_tag) return true;
+        if ((i & 63) == 63 && globaltimer_ns() - t0 > kWaitNs) return false;
+        __nanosleep(256);
+    }
+}
+
 __device__ __forceinline__ void issue_tile_ix(const Params &p, uint32_t t, uint8_t *dst, uint64_t *bar) {
+    if (p.arrive && !wait_arrival(p, t)) fail(p.hdr, ERR_TIMEOUT);
     constexpr int kBuf = kPre + kTile;
     const uint8_t *lo_full = p.abase + (uint64_t)t * kTile - kPre;
     const uint8_t *lo = t == 0 ? p.abase : lo_full;

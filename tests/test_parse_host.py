@@ -47,8 +47,12 @@ def parse_host(engine, doc, dialect, cols):
     return index[: out.n_index], hcols.rows, keep, [hcols.cols[k].str_len for k in range(len(cols))]
 
 
+# 80 MiB and up: the input is copied in chunks and the index kernel starts
+# on the first chunk (each tile waits for its own chunk's arrival flag).
 @pytest.mark.parametrize("kind,dialect,size", [(gen.CSV_HASH, fx.CSV_HASH, 4 << 20), (gen.ADVERSARIAL, fx.CSV_HASH, 3 << 20),
-                                               (gen.CSV_GEO, fx.CSV, 1 << 20), (gen.CSV_HASH, fx.CSV_HASH, 777)])
+                                               (gen.CSV_GEO, fx.CSV, 1 << 20), (gen.CSV_HASH, fx.CSV_HASH, 777),
+                                               (gen.CSV_HASH, fx.CSV_HASH, 80 << 20),
+                                               (gen.ADVERSARIAL, fx.CSV_HASH, (72 << 20) + 12345)])
 def test_parse_host_matches_oracle(engine, kind, dialect, size):
     doc = bytes(gen.generate(kind, size))
     for rep in range(2):  # the second call reuses the context's buffers and copy stream
