@@ -27,6 +27,8 @@ sys.path.insert(0, ROOT)
 GIB = float(1 << 30)
 SCHEMA_COLS = [(0, 1), (1, 3), (3, 1), (4, 2), (5, 2)]  # u32 id, str City, u32 pop, f64 lat, f64 lon
 METRIC = "device-resident parse GiB/s vs HBM peak; learned-speculative vs plain, bit-exact"
+WORKLOAD = ("csv_hash 1 GiB: structural index + field bytes + typed columns "
+            "(u32 id, str City, u32 population, f64 lat, f64 lon)")
 
 
 def peaks():
@@ -161,7 +163,7 @@ def bench_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GiB/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": "csv_hash 1 GiB: index + field bytes + typed columns (CPU sample)",
+            "config": {"workload": WORKLOAD, "input": "host memory; each step a CPU sample of the workload",
                        "sample_bytes": int(data.size)},
             "cpu_baseline": {"value": round(v, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
                              "sample": "%d-byte csv_hash document, full index + field bytes + columns" % data.size},
@@ -333,8 +335,7 @@ def bench_gpu(args):
         "metric": METRIC, "value": round(value, 4), "unit": "GiB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "csv_hash 1 GiB device-resident: structural index + field bytes + typed columns "
-                               "(u32 id, str City, u32 population, f64 lat, f64 lon)",
+        "config": {"workload": WORKLOAD, "input": "device-resident (value); pinned host buffers (e2e)",
                    "bytes": n, "structurals": int(n_struct), "rows": int(rows), "tile_bytes": 16384,
                    "l2": "input 1 GiB > L2, no flush", "parallelism": "replicas" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
