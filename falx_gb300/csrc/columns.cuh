@@ -331,7 +331,9 @@ __device__ __forceinline__ Rec make_rec(const ColParams &p, const Win &W, const 
     return x;
 }
 
-template <int D>
+// STATS: the count / sum sink is requested (its code is compiled only
+// into the kernels that need it: a smaller kernel fetches faster).
+template <int D, bool STATS>
 __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_constant__ ColParams p) {
     extern __shared__ __align__(16) uint8_t col_smem_raw[];
     ColSmem &S = *reinterpret_cast<ColSmem *>(col_smem_raw);
@@ -548,11 +550,11 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
         // memory for the block totals at the end
         StatAcc acc = {};
         uint32_t fb_fields = 0, fb_bytes = 0;  // below 2^32: the input is shorter than 4 GiB
-        if (rs.want_fb || rs.want_stats) {
+        if (rs.want_fb || STATS) {
             for (int li = tid - 32; li < kRecBlock; li += kThreads - 32) {
                 const Rec x = make_rec<D>(p, W, E, R0, li);
                 if (!x.row) continue;
-                if (rs.want_stats) {
+                if (STATS) {
                     acc.records++;
 #pragma unroll
                     for (int k = 0; k < 2; k++) {
@@ -568,7 +570,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
         }
         unsigned long long r[11] = {fb_fields, fb_bytes, acc.records, acc.values[0], acc.values[1], acc.checksum[0],
                                     acc.checksum[1], acc.sum_e6[0], acc.sum_e6[1], acc.inexact[0], acc.inexact[1]};
-        if (!rs.want_stats) {
+        if (!STATS) {
             uint32_t f = fb_fields, by = fb_bytes;
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) {
@@ -588,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
             for (int k = 0; k < 11; k++) S.red[warp][k] = r[k];
     }
     __syncthreads();
-    const int nred = rs.want_stats ? 11 : rs.want_fb ? 2 : 0;
+    const int nred = STATS ? 11 : rs.want_fb ? 2 : 0;
 
     // ---- cells, column by column (the records are read again from shared
     // memory: cheaper than keeping them in registers across the look-back)

@@ -808,9 +808,13 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     const size_t smem_cells = sizeof(ColSmem);
 #define FALX_COLS(D)                                                                                           \
     do {                                                                                                       \
-        FALX_CUDA(cudaFuncSetAttribute((const void *)columns_kernel<D>,                                        \
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cells));         \
-        if (grid) columns_kernel<D><<<(unsigned)grid, kThreads, smem_cells, c->stream>>>(cp);                  \
+        const void *fn_ = rs.want_stats ? (const void *)columns_kernel<D, true>                                \
+                                        : (const void *)columns_kernel<D, false>;                              \
+        FALX_CUDA(cudaFuncSetAttribute(fn_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cells));   \
+        if (grid && rs.want_stats)                                                                             \
+            columns_kernel<D, true><<<(unsigned)grid, kThreads, smem_cells, c->stream>>>(cp);                  \
+        else if (grid)                                                                                         \
+            columns_kernel<D, false><<<(unsigned)grid, kThreads, smem_cells, c->stream>>>(cp);                 \
         if (c->timing) cudaEventRecord(c->ev[2], c->stream);                                                   \
     } while (0)
     switch (dialect) {
