@@ -592,10 +592,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
     __syncthreads();
     const int nred = STATS ? 11 : rs.want_fb ? 2 : 0;
 
-    // ---- cells, column by column (the records are read again from shared
-    // memory: cheaper than keeping them in registers across the look-back)
-#pragma unroll
-    for (int i = 0; i < kRecPerThread; i++) rec[i] = make_rec<D>(p, W, E, R0, warp * 64 + i * 32 + lane);
+    // ---- cells, column by column
     const uint32_t row_base = S.row_base;
     const uint32_t wrow = S.warp_rows[warp];  // the warp's first row, block-relative
     uint32_t grow[kRecPerThread];             // file row of each record
