@@ -18,6 +18,7 @@
 #include <cstdint>
 
 #include "decimal.cuh"
+#include "swar.cuh"
 #include "rows.cuh"
 #include "scan_core.cuh"
 #include "tile.cuh"
@@ -143,42 +144,14 @@ __device__ __forceinline__ uint64_t lds_u64(const uint8_t *base, uint32_t o) {
     return (uint64_t)__funnelshift_r(a, b, sh) | ((uint64_t)__funnelshift_r(b, c, sh) << 32);
 }
 
-// Every byte of x that `keep` selects (0xFF per byte) is an ASCII digit.
-// Per byte b < 0x80: b + 0x46 reaches bit 7 iff b > '9'; (b | 0x80) - 0x30
-// keeps bit 7 iff b >= '0' and never borrows. Only a byte >= 0xBA carries
-// into the byte above it; such a byte fails the test itself when kept, and
-// the callers' unkept bytes are zero, or a digit and '.' checked elsewhere.
-__device__ __forceinline__ bool digits_ok(uint64_t x, uint64_t keep) {
-    constexpr uint64_t H = 0x8080808080808080ull;
-    const uint64_t bad = (x | (x + 0x4646464646464646ull) | ~((x | H) - 0x3030303030303030ull)) & H & keep;
-    return bad == 0;
-}
-// Four digits, the most significant in byte 0 (bytes '0'-'9' or 0):
-// pairs 10 a + b in bytes 0 and 2 (each at most 99: no carries), then
-// 100 x pair0 + pair1.
-__device__ __forceinline__ uint32_t four_digits(uint32_t w) {
-    w &= 0x0F0F0F0Fu;
-    w = w * 10u + (w >> 8);
-    return (w & 0xFFu) * 100u + ((w >> 16) & 0xFFu);
-}
-__device__ __forceinline__ uint32_t eight_digits(uint64_t x) {
-    return four_digits((uint32_t)x) * 10000u + four_digits((uint32_t)(x >> 32));
-}
-
-// 1-8 plain digits at shared offset o (str::parse::<u32> of such a cell).
+// 1-8 plain digits at shared offset o (swar.cuh).
 __device__ __forceinline__ bool swar_u32(const uint8_t *sd, uint32_t o, uint32_t n, uint32_t &v) {
     if (n - 1u > 7u) return false;
-    const uint32_t sh = 8u * (8u - n);
-    const uint64_t x = lds_u64(sd, o) << sh;  // the n bytes at the top, zeros below
-    if (!digits_ok(x, ~0ull << sh)) return false;
-    v = eight_digits(x);
-    return true;
+    return swar::u32_word(lds_u64(sd, o), n, v);
 }
 
-// [+-]?d{1,3}.d{6} at shared offset o: the mantissa m (integer and
-// fraction digits) and the f64 bits of m / 1e6, correctly rounded
-// (csv_geo.rs:1414-1475 divides in IEEE arithmetic; Eisel-Lemire gives the
-// same correctly rounded quotient with integer operations).
+// [+-]?d{1,3}.d{6} at shared offset o (swar.cuh): mantissa m, sign and the
+// f64 bits of m / 1e6.
 __device__ __forceinline__ bool swar_fixed6(const uint8_t *sd, uint32_t o, uint32_t n, uint64_t &bits, uint32_t &m,
                                             bool &neg) {
     if (n - 8u > 3u) return false;  // n in [8, 11]
@@ -186,16 +159,7 @@ __device__ __forceinline__ bool swar_fixed6(const uint8_t *sd, uint32_t o, uint3
     const uint32_t sg = (c0 == '-' || c0 == '+') ? 1u : 0u;
     const uint32_t k = n - 7u - sg;  // integer digits
     if (k - 1u > 2u) return false;
-    const uint64_t t = lds_u64(sd, o + n - 8u);  // last integer digit, '.', six fraction digits
-    const uint32_t ish = 8u * (4u - k);
-    const uint32_t u = lds_u32(sd, o + sg) << ish;  // the k integer digits at the top
-    if (((uint32_t)(t >> 8) & 0xFFu) != '.' || !digits_ok(t, 0xFFFFFFFFFFFF0000ull) ||
-        !digits_ok(u, (uint64_t)(0xFFFFFFFFu << ish)))
-        return false;
-    m = four_digits(u) * 1000000u + eight_digits(t & 0xFFFFFFFFFFFF0000ull);
-    neg = c0 == '-';
-    bits = dec::eisel_lemire(m, -6) | ((uint64_t)neg << 63);
-    return true;
+    return swar::fixed6_words(c0, k, lds_u64(sd, o + n - 8u), lds_u32(sd, o + sg), bits, m, neg);
 }
 
 // An unquoted staged cell copied to dst (any alignment): bytes up to a
@@ -208,7 +172,7 @@ __device__ __forceinline__ void copy_staged(const uint8_t *sd, uint32_t o, uint3
     for (; i < n; i++) dst[i] = sd[o + i];
 }
 
-// Select / add on a small per-thread array by a warp-uniform slot without
+// Select from a small per-thread array by a warp-uniform slot without
 // dynamic register indexing (which would move the array to local memory).
 template <typename T, int N>
 __device__ __forceinline__ T pick(const T (&a)[N], int k) {
@@ -216,11 +180,6 @@ __device__ __forceinline__ T pick(const T (&a)[N], int k) {
 #pragma unroll
     for (int j = 1; j < N; j++) x = k == j ? a[j] : x;
     return x;
-}
-template <typename T, int N>
-__device__ __forceinline__ void bump(T (&a)[N], int k, T v) {
-#pragma unroll
-    for (int j = 0; j < N; j++) a[j] += k == j ? v : (T)0;
 }
 
 // Cells the word-at-a-time paths do not take (other shapes, quoted
