@@ -16,6 +16,10 @@
  *  - Offsets are u32, so inputs must be shorter than 4 GiB
  *    (the reference's limit as well: csv_geo.rs push_indexes stores u32).
  *  - A context is single-stream and not thread-safe; use one per host thread.
+ *  - Device input is read in whole 16-byte-aligned chunks (bulk copies), so
+ *    the bytes of the chunks that hold data[0] and data[len-1] are read too;
+ *    they stay inside the allocation (CUDA allocations are at least 256-byte
+ *    aligned and granular) and never affect the results.
  */
 #ifndef FALX_GPU_H
 #define FALX_GPU_H
