@@ -29,7 +29,7 @@ constexpr int kRecPerThread = 2;
 constexpr int kRecBlock = kThreads * kRecPerThread;  // records per CTA
 constexpr int kRecWords = kRecBlock / 64 + 1;        // validity words a block's rows can touch
 constexpr int kSepWin = 3072;                        // separators staged per CTA
-constexpr int kDataWin = 32768;                      // bytes staged per CTA (cells pass)
+constexpr int kDataWin = 32768;                      // bytes staged per CTA
 
 // Look-back record of one record block, tagged with the call's epoch:
 // flag = epoch * 4 + 1 once the block's own sums are published, + 2 once
@@ -62,8 +62,8 @@ struct ColParams {
     RowSpec rows;
 };
 
-// Shared memory of one record block. The tape entries of its records and
-// (cells pass) the bytes they span are staged with coalesced loads; what
+// Shared memory of one record block. The tape entries of its records, their
+// separators and the bytes they span are staged with coalesced loads; what
 // does not fit the windows is read from global memory.
 struct ColSmem {
     alignas(16) uint64_t ends[kRecBlock + 2];  // ends[R0 - 2 + i]: 16-byte copies of even pairs
