@@ -1284,7 +1284,10 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     const bool index_done = c->host_index_done;
     c->host_index = nullptr;
     c->host_index_done = false;
-    if (index_done) FALX_CUDA(cudaStreamSynchronize(c->copy_stream));
+    // an early return inside parse_device leaves the chunk hand-off unused;
+    // either way the copies from host_data end before this call returns
+    c->pend_arrive = nullptr;
+    if (index_done || chunked) FALX_CUDA(cudaStreamSynchronize(c->copy_stream));
     if (rc && rc != FALX_ERR_CAPACITY) return rc;
     auto back = [&](void *dst, const void *src, uint64_t bytes) -> int {
         if (bytes && dst) FALX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
