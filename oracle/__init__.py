@@ -73,6 +73,16 @@ def lib():
         l.orc_par_columns.restype = c_int
         l.orc_par_columns.argtypes = [c_int, c_void_p, c_uint64, c_int, POINTER(orc_col), c_int, c_uint64,
                                       POINTER(c_uint64)]
+        l.orc_par_parse.restype = c_int
+        l.orc_par_parse.argtypes = [c_int, c_void_p, c_uint64, c_int, c_void_p, c_uint64, POINTER(c_uint64),
+                                    POINTER(orc_col), c_int, c_uint64, POINTER(c_uint64), POINTER(c_uint64),
+                                    POINTER(c_uint64), c_uint32, c_uint32, POINTER(orc_geo_stats)]
+        l.orc_par_ndjson_json.restype = c_int
+        l.orc_par_ndjson_json.argtypes = [c_void_p, c_uint64, c_int, POINTER(orc_ndjson_stats)]
+        l.orc_par_geo_stats.restype = None
+        l.orc_par_geo_stats.argtypes = [c_int, c_void_p, c_uint64, c_int, c_uint32, c_uint32, POINTER(orc_geo_stats)]
+        l.falx_gen.restype = c_uint64
+        l.falx_gen.argtypes = [c_int, c_uint64, c_uint64, c_void_p, c_uint64, c_int]
         l.orc_par_field_bytes.restype = None
         l.orc_par_field_bytes.argtypes = [c_int, c_void_p, c_uint64, c_int, POINTER(c_uint64), POINTER(c_uint64)]
         _lib = l
@@ -202,6 +212,32 @@ def parse_columns(data, dialect, columns, par_threads=0):
     return rows.value, _collect(columns, cols, keep, rows.value)
 
 
+def parse_par(data, dialect, columns, threads, index=True, field_bytes=True, stats_fields=None):
+    """Index, field bytes, columns and count / sum from one parallel pass
+    per chunk: {"index", "field_bytes", "rows", "columns", "stats"}."""
+    a, p, n = _buf(data)
+    rows_cap = n // 4 + 64
+    cols, keep = _alloc_cols(columns, rows_cap, n + 1)
+    idx = np.empty(n // 2 + 64, dtype=np.uint32) if index else None
+    ni, rows, f, b = c_uint64(), c_uint64(), c_uint64(), c_uint64()
+    st = orc_geo_stats() if stats_fields else None
+    sf = stats_fields or (0, 0)
+    rc = lib().orc_par_parse(dialect, p, n, threads, idx.ctypes.data_as(c_void_p) if index else None,
+                             idx.size if index else 0, byref(ni) if index else None, cols, len(columns), rows_cap,
+                             byref(rows), byref(f) if field_bytes else None, byref(b) if field_bytes else None,
+                             sf[0], sf[1], byref(st) if st is not None else None)
+    assert rc == 0
+    return {"index": idx[: ni.value] if index else None, "field_bytes": (f.value, b.value) if field_bytes else None,
+            "rows": rows.value, "columns": _collect(columns, cols, keep, rows.value), "stats": st}
+
+
+def geo_stats_par(data, dialect, f0, f1, threads):
+    a, p, n = _buf(data)
+    st = orc_geo_stats()
+    lib().orc_par_geo_stats(dialect, p, n, threads, f0, f1, byref(st))
+    return st
+
+
 def geo_stats(data, dialect, f0, f1):
     a, p, n = _buf(data)
     st = orc_geo_stats()
@@ -226,10 +262,10 @@ def ndjson_literal(data):
     return None if rc else (r.value, s.value)
 
 
-def ndjson_json(data):
+def ndjson_json(data, threads=0):
     a, p, n = _buf(data)
     st = orc_ndjson_stats()
-    rc = lib().orc_ndjson_json(p, n, byref(st))
+    rc = lib().orc_par_ndjson_json(p, n, threads, byref(st)) if threads else lib().orc_ndjson_json(p, n, byref(st))
     if rc:
         return None
     total = (int(st.total_e6_hi) << 64) | (int(st.total_e6_lo) & ((1 << 64) - 1))
@@ -253,3 +289,22 @@ def parse_u32(cell):
     v = c_uint32()
     a, p, n = _buf(cell)
     return v.value if lib().orc_parse_u32(p, n, byref(v)) else None
+
+
+# Seeded synthetic documents (the generator compiled into this library; the
+# same bytes as the package's generator for the same kind, size and seed).
+GEN_CSV_GEO, GEN_CSV_HASH, GEN_NDJSON, GEN_TSV, GEN_LOGFMT, GEN_ADVERSARIAL = 0, 1, 2, 3, 4, 5
+GEN_SEEDS = {0: 0xDEADBEEFCAFEBABE, 1: 0xC0FFEE15600DF00D, 2: 0x853C49E6748FEA9B, 3: 0xA0761D6478BD642F,
+             4: 0xE7037ED1A0B428DB, 5: 0x5EEDC5A51234ABCD}
+
+
+def generate(kind, target_bytes, seed=None, threads=None):
+    import os
+
+    seed = GEN_SEEDS[kind] if seed is None else seed
+    threads = threads or os.cpu_count() or 1
+    buf = np.empty(target_bytes + (1 << 20), dtype=np.uint8)
+    n = lib().falx_gen(kind, seed, target_bytes, buf.ctypes.data_as(c_void_p), buf.size, threads)
+    if n > buf.size:
+        raise ValueError("output buffer too small")
+    return buf[:n]

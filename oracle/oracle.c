@@ -7,6 +7,7 @@
 #include "oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -669,6 +670,24 @@ static void stats_record(void *vctx, const uint8_t *d, const orc_record *r) {
     }
 }
 
+/* One count / sum cell (the stats sink's per-cell work). */
+int orc_stats_cell(const uint8_t *raw, uint64_t len, uint64_t *bits, int64_t *e6, int *exact) {
+    uint8_t small[256];
+    uint8_t *scratch = len <= sizeof small ? small : (uint8_t *)malloc(len);
+    uint64_t vl;
+    const uint8_t *vs = numeric_view(raw, len, scratch, &vl);
+    double v;
+    int ok = orc_parse_f64(vs, vl, &v);
+    if (ok) {
+        union { double f; uint64_t u; } b;
+        b.f = v;
+        *bits = b.u;
+        *exact = exact_e6(vs, vl, e6);
+    }
+    if (scratch != small) free(scratch);
+    return ok;
+}
+
 void orc_geo_stats_run(int dialect, const uint8_t *d, uint64_t n, uint32_t field0, uint32_t field1,
                        orc_geo_stats *out) {
     memset(out, 0, sizeof *out);
@@ -867,6 +886,58 @@ static int find_member(const uint8_t *d, uint64_t e, uint64_t *i, const char *ke
         if (j < e && d[j] == ',') { j++; continue; }
         return 0;
     }
+}
+
+/* Parallel form: chunks snapped to the byte after a newline, totals added
+ * (records are independent lines, ndjson.rs:857-880). */
+typedef struct {
+    const uint8_t *d;
+    uint64_t lo, hi;
+    orc_ndjson_stats st;
+    int rc;
+} nd_job;
+
+static void *nd_part(void *arg) {
+    nd_job *j = (nd_job *)arg;
+    j->rc = orc_ndjson_json(j->d + j->lo, j->hi - j->lo, &j->st);
+    return NULL;
+}
+
+int orc_par_ndjson_json(const uint8_t *d, uint64_t n, int threads, orc_ndjson_stats *out) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    nd_job jobs[256];
+    pthread_t th[256];
+    uint64_t b[257];
+    b[0] = 0;
+    for (int t = 1; t < threads; t++) {
+        uint64_t x = n / (uint64_t)threads * (uint64_t)t;
+        if (x < b[t - 1]) x = b[t - 1];
+        const uint8_t *nl = x < n ? (const uint8_t *)memchr(d + x, '\n', n - x) : NULL;
+        b[t] = nl ? (uint64_t)(nl - d) + 1 : n;
+    }
+    b[threads] = n;
+    for (int t = 0; t < threads; t++) {
+        jobs[t].d = d;
+        jobs[t].lo = b[t];
+        jobs[t].hi = b[t + 1];
+        pthread_create(&th[t], NULL, nd_part, &jobs[t]);
+    }
+    __int128 total = 0;
+    int rc = 0;
+    memset(out, 0, sizeof *out);
+    for (int t = 0; t < threads; t++) {
+        pthread_join(th[t], NULL);
+        if (jobs[t].rc) rc = -1;
+        out->records += jobs[t].st.records;
+        out->sum_id = (int64_t)((uint64_t)out->sum_id + (uint64_t)jobs[t].st.sum_id);
+        out->sum_score_e6 = (int64_t)((uint64_t)out->sum_score_e6 + (uint64_t)jobs[t].st.sum_score_e6);
+        total += ((__int128)jobs[t].st.total_e6_hi << 64) | (__int128)(uint64_t)jobs[t].st.total_e6_lo;
+    }
+    out->total_e6_lo = (int64_t)(uint64_t)total;
+    out->total_e6_hi = (int64_t)(total >> 64);
+    out->total_f64 = (double)total / 1e6;
+    return rc;
 }
 
 int orc_ndjson_json(const uint8_t *d, uint64_t n, orc_ndjson_stats *out) {

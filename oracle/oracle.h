@@ -97,6 +97,10 @@ typedef struct {
     double total_f64;      /* (double)total_e6 / 1e6 */
 } orc_ndjson_stats;
 int orc_ndjson_json(const uint8_t *d, uint64_t n, orc_ndjson_stats *out);
+int orc_par_ndjson_json(const uint8_t *d, uint64_t n, int threads, orc_ndjson_stats *out);
+/* One count / sum cell: 1 if it holds a value (bits, and its exact x1e6
+ * value when it has one). */
+int orc_stats_cell(const uint8_t *raw, uint64_t len, uint64_t *bits, int64_t *e6, int *exact);
 
 /* Cell decoders with str::parse semantics. */
 int orc_parse_f64(const uint8_t *s, uint64_t len, double *out);
@@ -111,6 +115,16 @@ int orc_par_columns(int dialect, const uint8_t *d, uint64_t n, int threads, orc_
                     uint64_t rows_cap, uint64_t *rows_out);
 void orc_par_field_bytes(int dialect, const uint8_t *d, uint64_t n, int threads, uint64_t *fields,
                          uint64_t *bytes);
+/* Index, field bytes, columns and count / sum over fields sf0, sf1 from one
+ * pass per chunk (any of n_idx, fields, ncols, stats may be absent / 0).
+ * Returns -1 if an output was too small. */
+int orc_par_parse(int dialect, const uint8_t *d, uint64_t n, int threads, uint32_t *idx, uint64_t idx_cap,
+                  uint64_t *n_idx, orc_col *cols, int ncols, uint64_t rows_cap, uint64_t *rows_out, uint64_t *fields,
+                  uint64_t *bytes, uint32_t sf0, uint32_t sf1, orc_geo_stats *stats);
+/* Count / sum over fields f0, f1 (csv_geo.rs:1513-1561 parse_csv_geo_stats_par):
+ * per chunk, then added; `fold` is the chunks' folds added in order. */
+void orc_par_geo_stats(int dialect, const uint8_t *d, uint64_t n, int threads, uint32_t f0, uint32_t f1,
+                       orc_geo_stats *out);
 
 #ifdef __cplusplus
 }

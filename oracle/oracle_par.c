@@ -13,9 +13,16 @@
  *  - record ownership for the sinks: a chunk emits the records after its
  *    first terminator and finishes the record open at its end
  *    (csv_geo.rs:952-1000).
- * Kernels are portable 64-bit SWAR (no ISA intrinsics), so the port is
- * slower than the reference's AVX-512 / NEON code; it is a reported
- * baseline, not a target.
+ * Block classification: on aarch64 NEON byte compares with pairwise-add
+ * movemasks and the quote prefix XOR as one PMULL carry-less multiply (the
+ * reference's NEON tier, csv_geo.rs:2696, which also requires the AES/PMULL
+ * extension); elsewhere portable 64-bit SWAR. Cells: SWAR fast paths for
+ * plain u32 and [-]d{1,3}.d{6} f64 ahead of the full parsers, as the
+ * reference's parse_fixed_6_decimal_signed / parse_f64_cell do
+ * (csv_geo.rs:1313-1475). orc_par_parse runs the index, field-byte, column
+ * and count / sum sinks in one pass per chunk, as parse_columns_chunks_par
+ * does for columns (csv_hash.rs:1507-1601). It is a reported baseline, not
+ * a target.
  */
 #define _GNU_SOURCE
 #include <pthread.h>
@@ -23,6 +30,11 @@
 #include <string.h>
 
 #include "oracle.h"
+
+#if defined(__aarch64__) && defined(__ARM_NEON) && defined(__ARM_FEATURE_AES)
+#include <arm_neon.h>
+#define ORC_NEON 1
+#endif
 
 /* ------------------------------------------------------------------------- */
 /* SWAR block classification: bit i = (p[i] == c) for a 64-byte block.        */
@@ -46,6 +58,30 @@ typedef struct {
     uint64_t nl, sep, q, h, bs;
 } bmask;
 
+#ifdef ORC_NEON
+/* 64 compare results (0xFF / 0 bytes) -> a 64-bit mask in byte order. */
+static inline uint64_t nmask(uint8x16_t a, uint8x16_t b, uint8x16_t c, uint8x16_t d) {
+    static const uint8_t wts[16] = {1, 2, 4, 8, 16, 32, 64, 128, 1, 2, 4, 8, 16, 32, 64, 128};
+    const uint8x16_t w = vld1q_u8(wts);
+    uint8x16_t s0 = vpaddq_u8(vandq_u8(a, w), vandq_u8(b, w));
+    uint8x16_t s1 = vpaddq_u8(vandq_u8(c, w), vandq_u8(d, w));
+    s0 = vpaddq_u8(s0, s1);
+    s0 = vpaddq_u8(s0, s0);
+    return vgetq_lane_u64(vreinterpretq_u64_u8(s0), 0);
+}
+#define NEQ(ch) nmask(vceqq_u8(v0, vdupq_n_u8(ch)), vceqq_u8(v1, vdupq_n_u8(ch)), vceqq_u8(v2, vdupq_n_u8(ch)), \
+                      vceqq_u8(v3, vdupq_n_u8(ch)))
+static inline void classify_block(int dialect, const uint8_t *p, bmask *m) {
+    const uint8x16_t v0 = vld1q_u8(p), v1 = vld1q_u8(p + 16), v2 = vld1q_u8(p + 32), v3 = vld1q_u8(p + 48);
+    m->nl = NEQ('\n');
+    m->sep = dialect == ORC_TSV ? NEQ('\t') : dialect == ORC_LOGFMT ? (NEQ(' ') | NEQ('=')) :
+             dialect == ORC_NDJSON ? 0 : NEQ(',');
+    m->q = dialect == ORC_TSV ? 0 : NEQ('"');
+    m->h = dialect == ORC_CSV_HASH ? NEQ('#') : 0;
+    m->bs = (dialect == ORC_LOGFMT || dialect == ORC_NDJSON) ? NEQ('\\') : 0;
+}
+#undef NEQ
+#else
 static inline void classify_block(int dialect, const uint8_t *p, bmask *m) {
     uint64_t nl = 0, sep = 0, q = 0, h = 0, bs = 0;
     for (int k = 0; k < 8; k++) {
@@ -68,10 +104,16 @@ static inline void classify_block(int dialect, const uint8_t *p, bmask *m) {
     m->h = h;
     m->bs = bs;
 }
+#endif
 
 static inline uint64_t pxor(uint64_t x) {
+#ifdef ORC_NEON
+    /* carry-less multiply by all ones: bit i = XOR of bits 0..i */
+    return vgetq_lane_u64(vreinterpretq_u64_p128(vmull_p64((poly64_t)x, (poly64_t)~0ull)), 0);
+#else
     x ^= x << 1; x ^= x << 2; x ^= x << 4; x ^= x << 8; x ^= x << 16; x ^= x << 32;
     return x;
+#endif
 }
 
 static inline uint64_t rmask(unsigned from, unsigned to) {
@@ -366,6 +408,55 @@ static int fast_f64(const uint8_t *s, uint64_t len, double *out) {
     return 1;
 }
 
+/* Every byte of x is an ASCII digit: a byte above '9' reaches bit 7 when
+ * 0x46 is added, one below '0' when 0x30 is subtracted (a carry or borrow
+ * between bytes only comes from a byte that fails itself). */
+static inline int all_digits8(uint64_t x) {
+    return (((x + 0x4646464646464646ull) | (x - 0x3030303030303030ull)) & 0x8080808080808080ull) == 0;
+}
+/* Eight ASCII digits, the first in the low byte, as a number (pairwise
+ * multiply-and-add: digit pairs, then fours, then eight). */
+static inline uint32_t swar8(uint64_t x) {
+    x -= 0x3030303030303030ull;
+    x = (x * 10 + (x >> 8)) & 0x00FF00FF00FF00FFull;
+    x = (x * 100 + (x >> 16)) & 0x0000FFFF0000FFFFull;
+    return (uint32_t)((x * 10000 + (x >> 32)) & 0xFFFFFFFFull);
+}
+/* 1-8 plain digits. */
+static inline int swar_u32(const uint8_t *s, uint64_t len, uint32_t *out) {
+    if (len < 1 || len > 8) return 0;
+    uint64_t v = 0;
+    memcpy(&v, s, len);
+    const uint64_t x = len == 8 ? v : (v << (8 * (8 - len))) | (0x3030303030303030ull >> (8 * len));
+    if (!all_digits8(x)) return 0;
+    *out = swar8(x);
+    return 1;
+}
+/* [+-]?d{1,3}.d{6}: the integer mantissa over 1e6 in IEEE division, sign
+ * OR'd into bit 63 (csv_geo.rs:1313-1322, :1414-1475). */
+static inline int swar_fixed6(const uint8_t *s, uint64_t len, double *out) {
+    if (len < 8 || len > 11) return 0;
+    const uint64_t sg = s[0] == '-' || s[0] == '+';
+    const uint64_t k = len - 7 - sg; /* integer digits */
+    if (k < 1 || k > 3) return 0;
+    uint64_t t;
+    memcpy(&t, s + len - 8, 8); /* last integer digit, '.', six fraction digits */
+    if (((t >> 8) & 0xFF) != '.') return 0;
+    const uint64_t fr = (t & ~0xFFFFull) | 0x3030ull;
+    if (!all_digits8(fr)) return 0;
+    uint64_t ip = 0;
+    for (uint64_t i = 0; i < k; i++) {
+        const uint8_t c = s[sg + i];
+        if ((uint8_t)(c - '0') > 9) return 0;
+        ip = ip * 10 + (uint64_t)(c - '0');
+    }
+    union { double f; uint64_t u; } b;
+    b.f = (double)(ip * 1000000 + swar8(fr)) / 1e6;
+    b.u |= (uint64_t)(s[0] == '-') << 63;
+    *out = b.f;
+    return 1;
+}
+
 static uint64_t fb_len(const uint8_t *raw, uint64_t len) {
     if (len >= 2 && raw[0] == '"' && raw[len - 1] == '"') {
         uint64_t il = len - 2, o = 0, i = 0;
@@ -396,7 +487,11 @@ typedef struct {
     pcol cols[32];
     uint64_t rows, rcap;
     uint64_t fields, bytes;
-    int want_cols, want_fb;
+    int want_cols, want_fb, want_idx, want_stats;
+    uint32_t sf[2];   /* count / sum fields */
+    orc_geo_stats st; /* count / sum of the chunk */
+    uint32_t *ipart;  /* structural index of the chunk's own bytes */
+    uint64_t icnt, icap;
     /* concatenation */
     uint64_t row_at;
     uint64_t *arena_at;
@@ -424,6 +519,38 @@ static void grow_rows(sink_job *j) {
 static void emit_record(sink_job *j, const uint8_t *d, uint64_t rs, uint64_t end, const uint64_t *fs, const uint64_t *fe,
                         uint32_t nf) {
     if (j->pl->dialect == ORC_CSV_HASH && end > rs && d[rs] == '#') return;
+    if (j->want_stats) {
+        j->st.records++;
+        for (int k = 0; k < 2; k++) {
+            if (j->sf[k] >= nf) continue;
+            const uint8_t *raw = d + fs[j->sf[k]];
+            const uint64_t len = fe[j->sf[k]] - fs[j->sf[k]];
+            double v;
+            uint64_t bits;
+            int64_t e6;
+            int exact;
+            if (swar_fixed6(raw, len, &v)) { /* exact in micro-units */
+                union { double f; uint64_t u; } b;
+                b.f = v;
+                bits = b.u;
+                const uint64_t sg = raw[0] == '-' || raw[0] == '+';
+                int64_t mm = 0;
+                for (uint64_t i = sg; i < len; i++)
+                    if (raw[i] != '.') mm = mm * 10 + (raw[i] - '0');
+                e6 = raw[0] == '-' ? -mm : mm;
+                exact = 1;
+            } else if (!orc_stats_cell(raw, len, &bits, &e6, &exact)) {
+                continue;
+            }
+            union { double f; uint64_t u; } b;
+            b.u = bits;
+            j->st.values[k]++;
+            j->st.checksum[k] += bits;
+            j->st.fold[k] += b.f;
+            if (exact) j->st.sum_e6[k] = (int64_t)((uint64_t)j->st.sum_e6[k] + (uint64_t)e6);
+            else j->st.inexact[k]++;
+        }
+    }
     if (!j->want_cols) return;
     if (j->rows >= j->rcap) grow_rows(j);
     uint64_t r = j->rows++;
@@ -456,13 +583,13 @@ static void emit_record(sink_job *j, const uint8_t *d, uint64_t rs, uint64_t end
         }
         case ORC_U32: {
             uint32_t x = 0;
-            if (present) ok = orc_parse_u32(v, vl, &x);
+            if (present) ok = swar_u32(v, vl, &x) || orc_parse_u32(v, vl, &x);
             ((uint32_t *)c->vals)[r] = ok ? x : 0;
             break;
         }
         case ORC_F64: {
             double x = 0;
-            if (present) ok = fast_f64(v, vl, &x);
+            if (present) ok = swar_fixed6(v, vl, &x) || fast_f64(v, vl, &x);
             ((double *)c->vals)[r] = ok ? x : 0.0;
             break;
         }
@@ -522,6 +649,17 @@ static void *sink_chunk(void *arg) {
         uint64_t st, term;
         step(pl->dialect, &m, c, &st, &term);
         st &= live;
+        if (j->want_idx && off < e) {
+            uint64_t sti = e - off < 64 ? st & ((1ull << (e - off)) - 1) : st;
+            if (j->icnt + 64 > j->icap) {
+                j->icap = j->icap * 2 + 4096;
+                j->ipart = (uint32_t *)realloc(j->ipart, j->icap * 4);
+            }
+            while (sti) {
+                j->ipart[j->icnt++] = (uint32_t)(off + (uint64_t)__builtin_ctzll(sti));
+                sti &= sti - 1;
+            }
+        }
         while (st) {
             uint64_t bit = st & (0 - st);
             uint64_t pos = off + (uint64_t)__builtin_ctzll(st);
@@ -587,6 +725,7 @@ static void *sink_copy(void *arg) {
 }
 
 static void free_job(sink_job *j) {
+    free(j->ipart);
     for (int k = 0; k < j->ncols; k++) {
         free(j->cols[k].vals);
         free(j->cols[k].valid);
@@ -664,4 +803,122 @@ void orc_par_field_bytes(int dialect, const uint8_t *d, uint64_t n, int threads,
     free(pl);
     *fields = f;
     *bytes = b;
+}
+
+/* ------------------------------------------------------------------------- */
+/* One pass per chunk: structural index, field bytes, columns and count /    */
+/* sum together.                                                             */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    sink_job *j;
+    uint32_t *out;
+    uint64_t at, cap;
+} icopy_job;
+
+static void *icopy(void *arg) {
+    icopy_job *c = (icopy_job *)arg;
+    const uint64_t n = c->j->icnt;
+    if (c->at < c->cap) memcpy(c->out + c->at, c->j->ipart, (c->at + n <= c->cap ? n : c->cap - c->at) * 4);
+    return NULL;
+}
+
+static void add_stats(orc_geo_stats *to, const orc_geo_stats *s) {
+    to->records += s->records;
+    for (int k = 0; k < 2; k++) {
+        to->values[k] += s->values[k];
+        to->checksum[k] += s->checksum[k];
+        to->sum_e6[k] = (int64_t)((uint64_t)to->sum_e6[k] + (uint64_t)s->sum_e6[k]);
+        to->inexact[k] += s->inexact[k];
+        to->fold[k] += s->fold[k];
+    }
+}
+
+int orc_par_parse(int dialect, const uint8_t *d, uint64_t n, int threads, uint32_t *idx, uint64_t idx_cap,
+                  uint64_t *n_idx, orc_col *cols, int ncols, uint64_t rows_cap, uint64_t *rows_out, uint64_t *fields,
+                  uint64_t *bytes, uint32_t sf0, uint32_t sf1, orc_geo_stats *stats) {
+    plan_t *pl = (plan_t *)malloc(sizeof(plan_t));
+    make_plan(pl, dialect, d, n, threads);
+    sink_job *jobs = (sink_job *)calloc((size_t)pl->threads, sizeof(sink_job));
+    for (int t = 0; t < pl->threads; t++) {
+        jobs[t].pl = pl;
+        jobs[t].t = t;
+        jobs[t].ncols = ncols;
+        jobs[t].want_cols = ncols > 0;
+        jobs[t].want_fb = fields != NULL;
+        jobs[t].want_idx = n_idx != NULL;
+        jobs[t].want_stats = stats != NULL;
+        jobs[t].sf[0] = sf0;
+        jobs[t].sf[1] = sf1;
+        for (int k = 0; k < ncols; k++) {
+            jobs[t].cols[k].field = cols[k].field;
+            jobs[t].cols[k].type = cols[k].type;
+        }
+    }
+    run_threads(pl->threads, sink_chunk, jobs, sizeof(sink_job));
+    int over = 0;
+    if (n_idx) {
+        icopy_job ic[256];
+        uint64_t total = 0;
+        for (int t = 0; t < pl->threads; t++) {
+            ic[t].j = &jobs[t];
+            ic[t].out = idx;
+            ic[t].at = total;
+            ic[t].cap = idx_cap;
+            total += jobs[t].icnt;
+        }
+        run_threads(pl->threads, icopy, ic, sizeof(icopy_job));
+        *n_idx = total;
+        if (total > idx_cap) over = 1;
+    }
+    if (fields) {
+        uint64_t f = 0, b = 0;
+        for (int t = 0; t < pl->threads; t++) {
+            f += jobs[t].fields;
+            b += jobs[t].bytes;
+        }
+        *fields = f;
+        *bytes = b;
+    }
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        for (int t = 0; t < pl->threads; t++) add_stats(stats, &jobs[t].st);
+    }
+    uint64_t rows = 0;
+    if (ncols > 0) {
+        uint64_t *arena_at = (uint64_t *)calloc((size_t)pl->threads * 32, 8);
+        uint64_t alen[32] = {0};
+        for (int k = 0; k < ncols; k++) {
+            if (cols[k].valid) memset(cols[k].valid, 0, ((rows_cap + 63) / 64) * 8);
+            if (cols[k].type == ORC_STR && cols[k].values) ((int32_t *)cols[k].values)[0] = 0;
+        }
+        for (int t = 0; t < pl->threads; t++) {
+            jobs[t].row_at = rows;
+            jobs[t].arena_at = arena_at + 32 * t;
+            jobs[t].out = cols;
+            jobs[t].rows_cap = rows_cap;
+            for (int k = 0; k < ncols; k++) {
+                jobs[t].arena_at[k] = alen[k];
+                alen[k] += jobs[t].cols[k].alen;
+            }
+            rows += jobs[t].rows;
+        }
+        for (int k = 0; k < ncols; k++) {
+            cols[k].str_len = alen[k];
+            if (cols[k].type == ORC_STR && alen[k] > cols[k].str_cap) over = 1;
+        }
+        if (rows > rows_cap) over = 1;
+        run_threads(pl->threads, sink_copy, jobs, sizeof(sink_job));
+        free(arena_at);
+    }
+    if (rows_out) *rows_out = rows;
+    for (int t = 0; t < pl->threads; t++) free_job(&jobs[t]);
+    free(jobs);
+    free(pl);
+    return over ? -1 : 0;
+}
+
+void orc_par_geo_stats(int dialect, const uint8_t *d, uint64_t n, int threads, uint32_t f0, uint32_t f1,
+                       orc_geo_stats *out) {
+    orc_par_parse(dialect, d, n, threads, NULL, 0, NULL, NULL, 0, 0, NULL, NULL, NULL, f0, f1, out);
 }
