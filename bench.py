@@ -9,8 +9,15 @@ columns u32 id, City string arena, u32 population, f64 latitude and f64
 longitude. Inputs are seeded synthetic documents with the workload's shapes
 (falx_gb300/gen.py); 1 GiB is larger than L2, so no flush is needed.
 
---impl reference times the CPU port of the reference's parallel drivers
-(oracle/, all host threads) on a bounded sample of the same workload.
+Beside the headline step the same JSON line carries the csv-geo config
+(64 MiB, index + lat/lon columns + fused count/sum; L2 flushed between
+steps), the NDJSON config (1 GiB, sum(id + nested.score)), learned
+speculation and the batched documents. The CPU-baseline leg runs the CPU
+port of the reference's parallel drivers (oracle/, all host threads) over
+the same full inputs; its outputs are compared with the GPU's, and the
+result is the line's `parity` object.
+
+--impl reference times that CPU port on the headline workload, full size.
 """
 
 import argparse
@@ -109,37 +116,75 @@ def make_input(size):
     return gen.generate(gen.CSV_HASH, size)
 
 
-def cpu_sample(size):
-    from falx_gb300 import gen
-
-    return gen.generate(gen.CSV_HASH, size)
-
-
 def run_cpu(data, threads):
-    """One CPU step over `data`: the reference's parallel index, field bytes
-    and columns drivers (port)."""
+    """One CPU step over `data`: the port of the reference's parallel drivers
+    (chunk transfer functions, serial composition, then one pass per chunk
+    feeding the index, field-byte and column sinks). Returns the outputs."""
     import oracle
 
-    oracle.index_par(data, oracle.CSV_HASH, threads)
-    oracle.field_bytes(data, oracle.CSV_HASH, par_threads=threads)
-    oracle.parse_columns(data, oracle.CSV_HASH, SCHEMA_COLS, par_threads=threads)
+    return oracle.parse_par(data, oracle.CSV_HASH, SCHEMA_COLS, threads)
 
 
-def cpu_baseline(sample_bytes, threads, budget_s=20.0):
-    data = cpu_sample(sample_bytes)
-    run_cpu(data, threads)  # warm-up
+def cpu_isa():
+    import platform
+
+    m = platform.machine()
+    return "aarch64 NEON + PMULL" if m == "aarch64" else "%s portable 64-bit SWAR" % m
+
+
+def timed_best(fn, budget_s=20.0, max_reps=3):
+    """Best wall time of fn() after one warm-up call, and the last result."""
+    out = fn()
     t0 = time.perf_counter()
-    reps = 0
     best = None
-    while True:
+    for _ in range(max_reps):
         s = time.perf_counter()
-        run_cpu(data, threads)
+        out = fn()
         dt = time.perf_counter() - s
         best = dt if best is None else min(best, dt)
-        reps += 1
-        if time.perf_counter() - t0 > budget_s or reps >= 5:
+        if time.perf_counter() - t0 > budget_s:
             break
-    return data.size / GIB / best, data.size
+    return best, out
+
+
+def compare_columns(got_cols, want_cols, schema_cols, rows_got, rows_want, mism):
+    """Columns bit-for-bit (values, validity, offsets, arena)."""
+    import numpy as np
+
+    if rows_got != rows_want:
+        mism.append("rows %d != %d" % (rows_got, rows_want))
+        return
+    for k, (f, t) in enumerate(schema_cols):
+        g, w = got_cols[k], want_cols[k]
+        if not np.array_equal(g["valid"], w["valid"]):
+            mism.append("column %d validity" % k)
+        if t == 3:
+            if not np.array_equal(g["offsets"], w["offsets"]):
+                mism.append("column %d offsets" % k)
+            if g["data"] != w["data"]:
+                mism.append("column %d arena" % k)
+        elif not np.array_equal(g["values"].view(np.uint8), w["values"].view(np.uint8)):
+            mism.append("column %d values" % k)
+
+
+def host_columns(schema_cols, bufs, rows, str_lens):
+    """The GPU's column buffers as NumPy (copied once, after timing)."""
+    import numpy as np
+
+    out = []
+    words = (rows + 63) // 64
+    for k, (f, t) in enumerate(schema_cols):
+        v, valid, sd = bufs[k]
+        c = {"valid": valid[:words].cpu().numpy().view(np.uint64)}
+        if t == 3:
+            c["offsets"] = v[: rows + 1].cpu().numpy().view(np.int32)
+            c["data"] = sd[: str_lens[k]].cpu().numpy().tobytes()
+        elif t == 1:
+            c["values"] = v[:rows].cpu().numpy().view(np.uint32)
+        else:
+            c["values"] = v[:rows].cpu().numpy().view(np.uint64)
+        out.append(c)
+    return out
 
 
 def bench_reference(args):
@@ -147,11 +192,10 @@ def bench_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample = args.cpu_sample
     t_total = []
-    from falx_gb300 import gen
+    import oracle
 
-    data = gen.generate(gen.CSV_HASH, sample)
+    data = oracle.generate(oracle.GEN_CSV_HASH, args.size)
     for _ in range(args.warmup):
         run_cpu(data, threads)
     for _ in range(args.steps):
@@ -163,10 +207,12 @@ def bench_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GiB/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "input": "host memory; each step a CPU sample of the workload",
-                       "sample_bytes": int(data.size)},
+            "config": {"workload": WORKLOAD, "input": "host memory; each step the whole workload",
+                       "bytes": int(data.size)},
             "cpu_baseline": {"value": round(v, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
-                             "sample": "%d-byte csv_hash document, full index + field bytes + columns" % data.size},
+                             "isa": cpu_isa(), "same_config": True,
+                             "sample": "the full %d-byte csv_hash document: index + field bytes + columns, one pass "
+                                       "per chunk" % data.size},
             "e2e": {"value": round(v, 4), "unit": "GiB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -324,17 +370,40 @@ def bench_gpu(args):
            "ms_per_step": round(e2e_s * 1e3, 3), "ms_min_max": [round(min(e2e_t) * 1e3, 3), round(max(e2e_t) * 1e3, 3)],
            "calls": len(e2e_t)}
 
+    # The step's outputs, copied back once after timing, for the parity check.
+    gpu_out = None
+    if not args.no_cpu and rank == 0:
+        gpu_out = {"index": index[:n_struct].cpu().numpy().view(np.uint32), "field_bytes": (fb.fields, fb.bytes),
+                   "rows": int(rows),
+                   "columns": host_columns(SCHEMA_COLS, bufs, int(rows),
+                                           [cols.cols[k].str_len for k in range(len(SCHEMA_COLS))])}
+    del h_index, h_vals
+
+    geo = None if args.no_configs else bench_geo(eng, args, rank)
+    nd = None if args.no_configs else bench_ndjson(eng, args, rank)
     spec = None if args.no_spec else bench_speculation(eng, args)
     batched = None if args.no_batch else bench_batch(eng, args)
 
     if rank != 0:
         return
     cpu = None
+    parity = {"status": "unchecked", "why": "--no-cpu"}
     if not args.no_cpu:
+        # CPU baseline on the full workload; its outputs check the GPU's.
         threads = os.cpu_count() or 1
-        v, sb = cpu_baseline(args.cpu_sample, threads)
-        cpu = {"value": round(v, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
-               "sample": "%d-byte csv_hash document: parallel index + field bytes + columns" % sb}
+        best, ref = timed_best(lambda: run_cpu(host, threads))
+        cpu = {"value": round(n / GIB / best, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
+               "isa": cpu_isa(), "same_config": True,
+               "sample": "the full %d-byte csv_hash document: index + field bytes + columns, one pass per chunk" % n}
+        mism = []
+        if gpu_out["index"].size != ref["index"].size or not np.array_equal(gpu_out["index"], ref["index"]):
+            mism.append("structural index (%d vs %d entries)" % (gpu_out["index"].size, ref["index"].size))
+        if tuple(gpu_out["field_bytes"]) != tuple(ref["field_bytes"]):
+            mism.append("field bytes %s != %s" % (gpu_out["field_bytes"], ref["field_bytes"]))
+        compare_columns(gpu_out["columns"], ref["columns"], SCHEMA_COLS, gpu_out["rows"], ref["rows"], mism)
+        parity = {"status": "ok" if not mism else "mismatch", "mismatches": mism,
+                  "checked": "structural index, field bytes, rows, every column's values / validity / "
+                             "offsets / arena, bit for bit against the CPU port on the same 1 GiB input"}
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "GiB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -349,10 +418,13 @@ def bench_gpu(args):
                               "path / step time; traffic = DRAM bytes of the step's kernels"},
         "kernels": kernels,
         "cpu_baseline": cpu,
+        "parity": parity,
         "e2e": e2e,
         "gpu_launches": args.steps * len(STEP_KERNELS),
         "clocks": clk.summary(),
         "field_bytes": {"fields": fb.fields, "bytes": fb.bytes},
+        "csv_geo": geo,
+        "ndjson": nd,
         "learned_speculation": spec,
         "batched": batched,
         "wall_s": round(wall, 3),
@@ -361,6 +433,170 @@ def bench_gpu(args):
     eng.close()
     if dist:
         dist.destroy_process_group()
+
+
+def flush_l2(buf):
+    """Write a buffer larger than L2 (129 MB) on the current stream."""
+    buf.zero_()
+
+
+def bench_geo(eng, args, rank):
+    """csv-geo (CSV dialect, header row, 64 MiB, device-resident): one
+    falx_parse per step giving the structural index, lat / lon f64 columns
+    and the fused count / sum (csv_geo.rs:1513 parse_csv_geo_stats_par). The
+    input fits L2, so L2 is flushed before every timed step. The CPU port
+    runs the same work on the same input; outputs are compared."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import falx_gb300 as fx
+    from falx_gb300 import _lib, gen
+
+    size = 64 << 20
+    host = gen.generate(gen.CSV_GEO, size)
+    n = int(host.size)
+    data = torch.from_numpy(host.copy()).cuda()
+    cols_spec = [(4, fx.F64), (5, fx.F64)]
+    schema = fx.Schema(fx.CSV, cols_spec)
+    cs = schema.to_c()
+    idx_cap, rows_cap = n // 4 + 1024, n // 8 + 64
+    index = torch.empty(idx_cap, dtype=torch.int32, device="cuda")
+    bufs = eng.alloc_columns(schema, rows_cap, 0)
+    cols = eng.columns_struct(schema, bufs, rows_cap, 0)
+    st = _lib.falx_geo_stats()
+    out = _lib.falx_outputs()
+    out.index, out.index_cap = index.data_ptr(), idx_cap
+    out.columns = ctypes.pointer(cols)
+    out.stats = ctypes.pointer(st)
+    out.stats_fields[0], out.stats_fields[1] = 4, 5
+    stream = torch.cuda.current_stream()
+    eng.lib.falx_set_stream(eng.ctx, ctypes.c_void_p(stream.cuda_stream))
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        _lib.check(eng.lib.falx_parse(eng.ctx, ctypes.byref(cs), ctypes.c_void_p(data.data_ptr()), n,
+                                      ctypes.byref(out)), "falx_parse")
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per = []
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            flush_l2(flush)
+            ev0.record(stream)
+            step()
+            ev1.record(stream)
+            ev1.synchronize()
+            per.append(ev0.elapsed_time(ev1))
+    ms = sum(per) / len(per)
+    n_struct, rows = int(out.n_index), int(cols.rows)
+    words = (rows + 63) // 64
+    algo = n + 4 * n_struct + 16 * rows + 2 * 8 * words
+    peak, peak_kind = peaks()
+    res = {"workload": "csv-geo 64 MiB (CSV dialect, header row, 5% quoted City cells): structural index + "
+                       "lat / lon f64 columns + fused count / sum",
+           "value": round(n / GIB / (ms / 1e3), 3), "unit": "GiB/s", "ms": round(ms, 4), "bytes": n,
+           "structurals": n_struct, "rows": rows, "l2": "flushed before every step (512 MiB write)",
+           "roofline": {"bound": "hbm", "achieved": round(algo / (ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(algo / (ms / 1e3) / 1e9 / peak, 4), "algorithmic_bytes": algo,
+                        "peak_kind": peak_kind},
+           "stats": {"records": st.records, "values": list(st.values), "checksum": [hex(x) for x in st.checksum],
+                     "sum_e6": list(st.sum_e6), "sum_f64": list(st.sum_f64)},
+           "clocks": clk.summary()}
+    if rank != 0 or args.no_cpu:
+        return res
+    import oracle
+
+    g_idx = index[:n_struct].cpu().numpy().view(np.uint32)
+    g_cols = host_columns(cols_spec, bufs, rows, [0, 0])
+    threads = os.cpu_count() or 1
+
+    def cpu_run():
+        r = oracle.parse_par(host, oracle.CSV, cols_spec, threads, field_bytes=False, stats_fields=(4, 5))
+        return r["index"], r["rows"], r["columns"], r["stats"]
+
+    best, (w_idx, w_rows, w_cols, w_st) = timed_best(cpu_run)
+    fold = oracle.geo_stats(host, oracle.CSV, 4, 5).fold  # the sequential fold, row order
+    mism = []
+    if not np.array_equal(g_idx, w_idx):
+        mism.append("structural index")
+    compare_columns(g_cols, w_cols, cols_spec, rows, w_rows, mism)
+    if st.records != w_st.records or list(st.values) != list(w_st.values) or \
+            list(st.checksum) != list(w_st.checksum) or list(st.sum_e6) != list(w_st.sum_e6):
+        mism.append("count / sum stats")
+    for k in range(2):
+        if abs(st.sum_f64[k] - fold[k]) > 1e-12 * max(1.0, abs(fold[k])):
+            mism.append("sum_f64[%d] beyond 1e-12 relative of the sequential fold" % k)
+    res["parity"] = {"status": "ok" if not mism else "mismatch", "mismatches": mism,
+                     "checked": "index, lat / lon values and validity bit for bit; records, values, bit checksums "
+                                "and exact e6 sums equal; f64 sums within 1e-12 relative of the sequential fold"}
+    res["cpu_baseline"] = {"value": round(n / GIB / best, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
+                           "isa": cpu_isa(), "sample": "the same 64 MiB input: index + lat / lon columns + count / "
+                                                       "sum, one pass per chunk"}
+    return res
+
+
+def bench_ndjson(eng, args, rank):
+    """NDJSON (1 GiB, device-resident): records and sum(id + nested.score)
+    as exact fixed-point totals and an f64 total per step
+    (ndjson.rs:726 parse_ndjson_id_score_par, JSON-aware). The CPU port's
+    JSON-aware sink runs on the same input; totals are compared."""
+    import torch
+
+    from falx_gb300 import gen
+
+    host = gen.generate(gen.NDJSON, args.size)
+    n = int(host.size)
+    data = torch.from_numpy(host.copy()).cuda()
+    stream = torch.cuda.current_stream()
+    eng._sync_stream()
+    for _ in range(max(3, args.warmup)):
+        r = eng.ndjson_id_score(data)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per = []
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            ev0.record(stream)
+            r = eng.ndjson_id_score(data)
+            ev1.record(stream)
+            ev1.synchronize()
+            per.append(ev0.elapsed_time(ev1))
+    ms = sum(per) / len(per)
+    peak, peak_kind = peaks()
+    res = {"workload": "NDJSON 1 GiB (id int64 < 2^40, name with escapes, nested.score decimal with 1-6 "
+                       "fraction digits, tags, active; 0-2 spaces around ':' and ','): records, sum(id + "
+                       "nested.score) exact and f64",
+           "value": round(n / GIB / (ms / 1e3), 3), "unit": "GiB/s", "ms": round(ms, 4), "bytes": n,
+           "records": int(r.records), "total_f64": r.total_f64, "l2": "input 1 GiB > L2, no flush",
+           "roofline": {"bound": "hbm", "achieved": round(n / (ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(n / (ms / 1e3) / 1e9 / peak, 4), "algorithmic_bytes": n,
+                        "peak_kind": peak_kind},
+           "clocks": clk.summary()}
+    if rank != 0 or args.no_cpu:
+        return res
+    import oracle
+
+    threads = os.cpu_count() or 1
+    best, want = timed_best(lambda: oracle.ndjson_json(host, threads=threads))
+    mism = []
+    if want is None:
+        mism.append("the CPU sink rejected the input")
+    else:
+        if r.records != want["records"] or r.sum_id != want["sum_id"] or r.sum_score_e6 != want["sum_score_e6"]:
+            mism.append("records / sums")
+        if r.total_e6 != want["total_e6"]:
+            mism.append("exact total")
+        if abs(r.total_f64 - want["total_f64"]) > 1e-12 * max(1.0, abs(want["total_f64"])):
+            mism.append("f64 total beyond 1e-12 relative")
+    res["parity"] = {"status": "ok" if not mism else "mismatch", "mismatches": mism,
+                     "checked": "records, wrapping id and score sums, exact 128-bit total; f64 total within "
+                                "1e-12 relative"}
+    res["cpu_baseline"] = {"value": round(n / GIB / best, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
+                           "sample": "the same 1 GiB input, JSON-aware sink, lines split across the threads"}
+    return res
 
 
 def bench_speculation(eng, args):
@@ -496,10 +732,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="falx_gb300")
     ap.add_argument("--size", type=int, default=1 << 30)
-    ap.add_argument("--cpu-sample", type=int, default=64 << 20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-spec", action="store_true", help="skip the learned-speculation comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-documents run")
+    ap.add_argument("--no-configs", action="store_true", help="skip the csv-geo and NDJSON configs")
     args = ap.parse_args()
     if args.impl == "reference":
         bench_reference(args)
