@@ -27,6 +27,8 @@ struct falx_ctx {
     int sm_count = 0;
     int blocks_per_sm[5][2] = {};
     int blocks_per_sm_spec[5] = {};
+    int blocks_per_sm_pass[5] = {};  // index_pass_kernel
+    int old_index = 0;               // FALX_INDEX_KERNEL=tile: plain scans use index_kernel instead
     int ctas_per_sm = 0;  // FALX_CTAS_PER_SM caps the persistent grid (tuning)
     falx::TileStatus *status = nullptr;
     falx::ArenaStatus *astatus = nullptr;
@@ -74,6 +76,7 @@ struct falx_ctx {
     uint64_t rec_sums_cap = 0;      // bytes
     uint32_t col_epoch = 0;         // their tag
     uint64_t stall_test_ns = 0;     // falx_test_stalled_lookback
+    int col_grid[5][2] = {};        // persistent columns grid per dialect, without / with the count-sum sink
     // per-launch timing of the last rows call (FALX_OPT_TIMING)
     int timing = 0;
     cudaEvent_t ev[5] = {};

@@ -34,6 +34,7 @@
 
 #include "tile.cuh"
 #include "columns.cuh"
+#include "index_pass.cuh"
 
 namespace falx {
 
@@ -575,6 +576,16 @@ int setup_spec_kernel(falx_ctx *c) {
     return FALX_OK;
 }
 
+template <int D>
+int setup_pass_kernel(falx_ctx *c) {
+    const void *fn = (const void *)index_pass_kernel<D>;
+    FALX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(IxSmem)));
+    int nb = 0;
+    FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kIxThreads, sizeof(IxSmem)));
+    c->blocks_per_sm_pass[D] = nb > 0 ? nb : 1;
+    return FALX_OK;
+}
+
 template <int D, bool ROWS>
 int setup_kernel(falx_ctx *c) {
     const void *fn = ROWS ? (const void *)scan_kernel<D, true> : (const void *)index_kernel<D>;
@@ -609,8 +620,9 @@ int ensure_status(falx_ctx *c, uint32_t tiles) {
 
 bool valid_dialect(int d) { return d >= FALX_CSV && d <= FALX_NDJSON; }
 
-// Launch the scan over [data, data+len) with the outputs in `P` (device).
-int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t len, Params P, bool spec = false) {
+// Launch the scan over [data, data+len) with the outputs in `P` (device);
+// the header (counts, error bits) is final once the stream reaches this point.
+int launch_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t len, Params P, bool spec = false) {
     uint64_t shift = (uint64_t)((uintptr_t)data & 15u);
     uint64_t tiles64 = (len + shift + kTile - 1) / kTile;
     uint32_t tiles = (uint32_t)tiles64;
@@ -627,7 +639,9 @@ int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t 
     P.astatus = c->astatus;
     P.hdr = c->hdr;
     P.halo = rows ? kHaloBytes : 0;
-    int nb = spec ? c->blocks_per_sm_spec[dialect] : c->blocks_per_sm[dialect][rows ? 1 : 0];
+    const bool pass = !rows && !spec && !c->old_index;
+    int nb = spec ? c->blocks_per_sm_spec[dialect] : pass ? c->blocks_per_sm_pass[dialect]
+                                                         : c->blocks_per_sm[dialect][rows ? 1 : 0];
     if (c->ctas_per_sm > 0 && c->ctas_per_sm < nb) nb = c->ctas_per_sm;
     uint64_t grid = (uint64_t)c->sm_count * (uint64_t)nb;
     if (grid > tiles) grid = tiles;
@@ -641,6 +655,9 @@ int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t 
         else if (spec)                                                                            \
             err = cudaLaunchCooperativeKernel((const void *)index_kernel<D, true>, dim3((unsigned)grid), \
                                               dim3(kThreads), args_, sizeof(SmemIx), c->stream);         \
+        else if (pass)                                                                            \
+            err = cudaLaunchCooperativeKernel((const void *)index_pass_kernel<D>, dim3((unsigned)grid), \
+                                              dim3(kIxThreads), args_, sizeof(IxSmem), c->stream);       \
         else                                                                                      \
             err = cudaLaunchCooperativeKernel((const void *)index_kernel<D>, dim3((unsigned)grid),     \
                                               dim3(kThreads), args_, sizeof(SmemIx), c->stream);         \
@@ -655,12 +672,22 @@ int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t 
     }
     FALX_CUDA(err);
 #undef FALX_LAUNCH
+    return FALX_OK;
+}
+
+// Header back to the host, then the call's error status.
+int finish_scan(falx_ctx *c) {
     FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
     FALX_CUDA(cudaStreamSynchronize(c->stream));
     if (c->hhdr->error & ERR_TIMEOUT) return FALX_ERR_TIMEOUT;
     if (c->hhdr->error & ERR_TMA) return FALX_ERR_TIMEOUT;
     if (c->hhdr->error & ERR_ARENA) return FALX_ERR_OVERFLOW;
     return FALX_OK;
+}
+
+int run_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t len, Params P, bool spec = false) {
+    const int rc = launch_scan(c, dialect, rows, data, len, P, spec);
+    return rc ? rc : finish_scan(c);
 }
 
 int check_common(falx_ctx *c, int dialect, const void *data, uint64_t len) {
@@ -714,27 +741,29 @@ int grow_scratch(void **p, uint64_t *cap, uint64_t need) {
 }
 
 // Rows, field bytes and count / sum from the tape: the index kernel writes
-// the tape (the caller's buffers when they are large enough, else scratch),
-// then columns_kernel decodes the records. P carries the caller's index and
-// tape outputs; rs the columns and sinks.
-int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, Params P) {
-    uint32_t *seps = P.seps;
-    uint64_t *ends = P.ends;
-    uint64_t scap = P.seps_cap, ecap = P.ends_cap;
-    const bool own = !seps || !ends;
-    if (own) {
-        // first guess from the input size; grown and re-run if too small
-        uint64_t gs = (len / 6 + 1024) * 4, ge = (len / 24 + 1024) * 8;
-        if (c->tape_seps_cap > gs) gs = c->tape_seps_cap;
-        if (c->tape_ends_cap > ge) ge = c->tape_ends_cap;
-        int rc = grow_scratch((void **)&c->tape_seps, &c->tape_seps_cap, gs);
-        if (!rc) rc = grow_scratch((void **)&c->tape_ends, &c->tape_ends_cap, ge);
-        if (rc) return rc;
-        P.seps = c->tape_seps;
-        P.seps_cap = c->tape_seps_cap / 4;
-        P.ends = c->tape_ends;
-        P.ends_cap = c->tape_ends_cap / 8;
+// the tape (the caller's buffers when it gives them, else scratch), then
+// columns_kernel decodes the records. The columns kernel reads the record
+// counts on the device, so the host waits once, after both launches, except
+// for host-buffer calls, which copy the index back while the columns kernel
+// runs and so need its size first. A tape that outgrew its buffers is
+// flagged by the columns kernel; both passes then run again with buffers of
+// the exact size. P carries the caller's index and tape outputs; rs the
+// columns and sinks.
+template <int D, bool STATS>
+int columns_grid(falx_ctx *c) {
+    int &g = c->col_grid[D][STATS ? 1 : 0];
+    if (!g) {
+        const void *fn = (const void *)columns_kernel<D, STATS>;
+        FALX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ColSmem)));
+        int nb = 0;
+        FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, sizeof(ColSmem)));
+        g = c->sm_count * (nb > 0 ? nb : 1);
     }
+    return FALX_OK;
+}
+
+int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, Params P) {
+    const bool own = !P.seps || !P.ends;
     const RowSpec rs = P.rows;
     memset(&P.rows, 0, sizeof P.rows);
     if (c->pend_arrive) {
@@ -744,94 +773,104 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
         c->pend_arrive = nullptr;
     }
     c->last_n = 0;
-    if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[0], c->stream));
-    int rc = run_scan(c, dialect, false, data, len, P);
-    if (rc) return rc;
-    uint64_t n_struct = c->hhdr->n_struct, n_terms = c->hhdr->n_terms;
-    if (n_struct - n_terms > P.seps_cap || n_terms > P.ends_cap) {
-        // the tape did not fit: index once more into scratch of the exact size
-        rc = grow_scratch((void **)&c->tape_seps, &c->tape_seps_cap, (n_struct - n_terms + 1) * 4);
-        if (!rc) rc = grow_scratch((void **)&c->tape_ends, &c->tape_ends_cap, (n_terms + 1) * 8);
+    // tape scratch: a first guess from the input size, the exact size after
+    // a pass that did not fit
+    uint64_t want_seps = (len / 6 + 1024) * 4, want_ends = (len / 24 + 1024) * 8;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        if (own) {
+            int rc = grow_scratch((void **)&c->tape_seps, &c->tape_seps_cap, want_seps);
+            if (!rc) rc = grow_scratch((void **)&c->tape_ends, &c->tape_ends_cap, want_ends);
+            if (rc) return rc;
+            P.seps = c->tape_seps;
+            P.seps_cap = c->tape_seps_cap / 4;
+            P.ends = c->tape_ends;
+            P.ends_cap = c->tape_ends_cap / 8;
+        }
+        if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[0], c->stream));
+        int rc = launch_scan(c, dialect, false, data, len, P);
         if (rc) return rc;
-        P.index = nullptr;
-        P.index_cap = 0;
-        P.arrive = nullptr;
-        P.seps = c->tape_seps;
-        P.seps_cap = c->tape_seps_cap / 4;
-        P.ends = c->tape_ends;
-        P.ends_cap = c->tape_ends_cap / 8;
-        rc = run_scan(c, dialect, false, data, len, P);
-        if (rc) return rc;
-    }
-    if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[1], c->stream));
-    if (c->host_index && P.index) {
-        // the index is final (the host has waited for the index kernel):
-        // copy it back while the columns kernel runs
-        const uint64_t ni = n_struct < c->host_index_cap ? n_struct : c->host_index_cap;
-        if (ni) FALX_CUDA(cudaMemcpyAsync(c->host_index, P.index, ni * 4, cudaMemcpyDeviceToHost, c->copy_stream));
-        c->host_index_done = true;
-    }
-    ColParams cp;
-    memset(&cp, 0, sizeof cp);
-    cp.data = data;
-    cp.shift = (uint32_t)((uintptr_t)data & 15u);
-    cp.abase = data - cp.shift;
-    cp.len = len;
-    cp.seps = P.seps;
-    cp.n_seps = n_struct - n_terms;
-    cp.ends = P.ends;
-    cp.n_ends = n_terms;
-    cp.n_recs = n_terms + 1;
-    cp.hdr = c->hdr;
-    cp.rows = rs;
-    const uint64_t blocks = (cp.n_recs + kRecBlock - 1) / kRecBlock;
-    // look-back records, tagged with a per-call epoch: cleared only when
-    // (re)allocated and when the epoch wraps
-    if (blocks * sizeof(BlkStatus) > c->rec_sums_cap || c->col_epoch >= (1u << 29)) {
-        rc = grow_scratch(&c->rec_sums, &c->rec_sums_cap, blocks * sizeof(BlkStatus));
-        if (rc) return rc;
-        FALX_CUDA(cudaMemsetAsync(c->rec_sums, 0, c->rec_sums_cap, c->stream));
-        c->col_epoch = 0;
-    }
-    cp.status = static_cast<BlkStatus *>(c->rec_sums);
-    cp.epoch = ++c->col_epoch;
-    cp.n_blocks = (uint32_t)blocks;
-    cp.wait_ns = kWaitNs;
-    uint64_t grid = blocks;
-    if (c->stall_test_ns) {
-        // test hook: run record block 1 alone, so its look-back waits for a
-        // block 0 that never publishes and gives up after the given limit
-        cp.blk0 = 1;
-        cp.wait_ns = c->stall_test_ns;
-        grid = blocks > 1 ? 1 : 0;
-    }
-    const size_t smem_cells = sizeof(ColSmem);
-#define FALX_COLS(D)                                                                                           \
-    do {                                                                                                       \
-        const void *fn_ = rs.want_stats ? (const void *)columns_kernel<D, true>                                \
-                                        : (const void *)columns_kernel<D, false>;                              \
-        FALX_CUDA(cudaFuncSetAttribute(fn_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cells));   \
-        if (grid && rs.want_stats)                                                                             \
-            columns_kernel<D, true><<<(unsigned)grid, kThreads, smem_cells, c->stream>>>(cp);                  \
-        else if (grid)                                                                                         \
-            columns_kernel<D, false><<<(unsigned)grid, kThreads, smem_cells, c->stream>>>(cp);                 \
-        if (c->timing) cudaEventRecord(c->ev[2], c->stream);                                                   \
+        if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[1], c->stream));
+        if (c->host_index && P.index) {
+            // host-buffer call: the index is final once the index kernel is
+            // done; copy it back while the columns kernel runs
+            rc = finish_scan(c);
+            if (rc) return rc;
+            const uint64_t n_struct = c->hhdr->n_struct;
+            const uint64_t ni = n_struct < c->host_index_cap ? n_struct : c->host_index_cap;
+            if (ni) FALX_CUDA(cudaMemcpyAsync(c->host_index, P.index, ni * 4, cudaMemcpyDeviceToHost, c->copy_stream));
+            c->host_index_done = true;
+        }
+        ColParams cp;
+        memset(&cp, 0, sizeof cp);
+        cp.data = data;
+        cp.shift = (uint32_t)((uintptr_t)data & 15u);
+        cp.abase = data - cp.shift;
+        cp.len = len;
+        cp.seps = P.seps;
+        cp.seps_cap = P.seps_cap;
+        cp.ends = P.ends;
+        cp.ends_cap = P.ends_cap;
+        cp.hdr = c->hdr;
+        cp.rows = rs;
+        // look-back records for every block the tape's capacity allows,
+        // tagged with a per-call epoch: cleared only when (re)allocated and
+        // when the epoch wraps
+        const uint64_t blocks = (P.ends_cap + 1 + kRecBlock - 1) / kRecBlock;
+        if (blocks * sizeof(BlkStatus) > c->rec_sums_cap || c->col_epoch >= (1u << 29)) {
+            rc = grow_scratch(&c->rec_sums, &c->rec_sums_cap, blocks * sizeof(BlkStatus));
+            if (rc) return rc;
+            FALX_CUDA(cudaMemsetAsync(c->rec_sums, 0, c->rec_sums_cap, c->stream));
+            c->col_epoch = 0;
+        }
+        cp.status = static_cast<BlkStatus *>(c->rec_sums);
+        cp.epoch = ++c->col_epoch;
+        cp.wait_ns = kWaitNs;
+        const size_t smem_cells = sizeof(ColSmem);
+#define FALX_COLS(D)                                                                                       \
+    do {                                                                                                   \
+        rc = rs.want_stats ? columns_grid<D, true>(c) : columns_grid<D, false>(c);                         \
+        if (rc) return rc;                                                                                 \
+        unsigned grid_ = (unsigned)c->col_grid[D][rs.want_stats ? 1 : 0];                                  \
+        if (c->stall_test_ns) {                                                                            \
+            /* test hook: one CTA starting at record block 1, so its look-back                          \
+               waits for a block 0 that never publishes and gives up after the                          \
+               given limit */                                                                              \
+            cp.blk0 = 1;                                                                                   \
+            cp.wait_ns = c->stall_test_ns;                                                                 \
+            grid_ = 1;                                                                                     \
+        }                                                                                                  \
+        if (rs.want_stats) columns_kernel<D, true><<<grid_, kThreads, smem_cells, c->stream>>>(cp);       \
+        else columns_kernel<D, false><<<grid_, kThreads, smem_cells, c->stream>>>(cp);                    \
     } while (0)
-    switch (dialect) {
-    case FALX_CSV: FALX_COLS(D_CSV); break;
-    case FALX_CSV_HASH: FALX_COLS(D_CSV_HASH); break;
-    case FALX_TSV: FALX_COLS(D_TSV); break;
-    default: FALX_COLS(D_LOGFMT); break;
-    }
+        switch (dialect) {
+        case FALX_CSV: FALX_COLS(D_CSV); break;
+        case FALX_CSV_HASH: FALX_COLS(D_CSV_HASH); break;
+        case FALX_TSV: FALX_COLS(D_TSV); break;
+        default: FALX_COLS(D_LOGFMT); break;
+        }
 #undef FALX_COLS
-    FALX_CUDA(cudaGetLastError());
-    FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
-    FALX_CUDA(cudaStreamSynchronize(c->stream));
+        FALX_CUDA(cudaGetLastError());
+        if (c->timing) FALX_CUDA(cudaEventRecord(c->ev[2], c->stream));
+        FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
+        FALX_CUDA(cudaStreamSynchronize(c->stream));
+        if (c->hhdr->error & (ERR_TIMEOUT | ERR_TMA)) return FALX_ERR_TIMEOUT;
+        if (!(c->hhdr->error & ERR_TAPE)) break;
+        if (!own || attempt == 1) return FALX_ERR_CAPACITY;  // the caller's tape buffers are too small
+        // the tape did not fit the scratch: size it exactly and run again
+        const uint64_t n_struct = c->hhdr->n_struct, n_terms = c->hhdr->n_terms;
+        want_seps = (n_struct - n_terms + 1) * 4;
+        want_ends = (n_terms + 1) * 8;
+        P.arrive = nullptr;  // the input is in place now
+        c->host_index_done = false;
+        for (int k = 0; k < rs.ncols; k++) {
+            const uint64_t words = (rs.rows_cap + 63) / 64;
+            if (words) FALX_CUDA(cudaMemsetAsync(rs.valid[k], 0, words * 8, c->stream));
+        }
+    }
     if (c->timing) {
         for (int k = 0; k < 2; k++) cudaEventElapsedTime(&c->last_ms[k], c->ev[k], c->ev[k + 1]);
         c->last_n = 2;
     }
-    if (c->hhdr->error & (ERR_TIMEOUT | ERR_TMA)) return FALX_ERR_TIMEOUT;
     for (int k = 0; k < kMaxStr; k++)
         if (c->hhdr->arena[k] > 0x7FFFFFFFull) return FALX_ERR_OVERFLOW;  // i32 string offsets
     return FALX_OK;
@@ -892,7 +931,7 @@ int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, ui
     }
     if (rows && c->rows_path == 0) rc = rows_two_pass(c, dialect, data, len, P);
     else rc = run_scan(c, dialect, rows, data, len, P);
-    if (rc) return rc;
+    if (rc && rc != FALX_ERR_CAPACITY) return rc;  // on CAPACITY the counts are still reported
     const DevHeader &h = *c->hhdr;
     o->n_index = h.n_struct;
     o->n_ends = h.n_terms;
@@ -926,7 +965,7 @@ int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, ui
             s.sum_f64[k] = (double)(int64_t)h.st_sum_e6[k] / 1e6;
         }
     }
-    return cap_err ? FALX_ERR_CAPACITY : FALX_OK;
+    return cap_err || rc ? FALX_ERR_CAPACITY : FALX_OK;
 }
 
 }  // namespace
@@ -955,12 +994,14 @@ int falx_create(int device, falx_ctx **out) {
     if (!c) return FALX_ERR_INVALID;
     c->device = device;
     if (const char *e = getenv("FALX_CTAS_PER_SM")) c->ctas_per_sm = atoi(e);
+    if (const char *e = getenv("FALX_INDEX_KERNEL")) c->old_index = strcmp(e, "tile") == 0;
     int rc = FALX_OK;
     if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) rc = FALX_ERR_CUDA;
 #define FALX_SETUP(D)                                  \
     if (!rc) rc = setup_kernel<D, false>(c);           \
     if (!rc) rc = setup_kernel<D, true>(c);            \
-    if (!rc) rc = setup_spec_kernel<D>(c);
+    if (!rc) rc = setup_spec_kernel<D>(c);             \
+    if (!rc) rc = setup_pass_kernel<D>(c);
     FALX_SETUP(D_CSV) FALX_SETUP(D_CSV_HASH) FALX_SETUP(D_TSV) FALX_SETUP(D_LOGFMT) FALX_SETUP(D_NDJSON)
 #undef FALX_SETUP
     if (!rc && cudaMalloc(&c->hdr, sizeof(DevHeader)) != cudaSuccess) rc = FALX_ERR_CUDA;

@@ -47,9 +47,13 @@ struct DevHeader {
     unsigned long long fb_fields, fb_bytes;
     unsigned long long st_records, st_values[2], st_checksum[2], st_sum_e6[2], st_inexact[2];
     unsigned long long spec_repairs;  // speculative tiles whose assumed entry state was wrong
+    uint32_t col_ticket;              // record blocks taken by the columns pass
+    uint32_t pad2;
 };
 
-enum : uint32_t { ERR_TIMEOUT = 1, ERR_ARENA = 2, ERR_TMA = 4 };
+// ERR_TAPE: the tape outgrew the buffers it was written to (the host sizes
+// them exactly and runs again)
+enum : uint32_t { ERR_TIMEOUT = 1, ERR_ARENA = 2, ERR_TMA = 4, ERR_TAPE = 8 };
 
 struct Params {
     const uint8_t *data;
