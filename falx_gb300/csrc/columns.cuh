@@ -4,7 +4,7 @@
 // terminated record `(separators before << 32) | terminator offset` in
 // `ends` (csv_geo.rs:1838-1849 push_tape). A record's fields are then a
 // contiguous run of `seps`, so every record can be decoded independently.
-// One launch: CTA b owns the 512 records [512 b, 512 b + 512). It stages
+// Record block b holds the 512 records [512 b, 512 b + 512). Its CTA stages
 // their tape entries and bytes, counts its rows (csv_hash comment records
 // are not rows, csv_hash.rs:1381) and the cleaned bytes of its string
 // cells, publishes those sums, and finds the sums of the blocks before it
@@ -49,14 +49,12 @@ struct ColParams {
     uint32_t shift;        // data - abase
     uint64_t len;
     const uint32_t *seps;
-    uint64_t n_seps;
+    uint64_t seps_cap;
     const uint64_t *ends;
-    uint64_t n_ends;
-    uint64_t n_recs;  // n_ends, plus one for a trailing record without terminator
+    uint64_t ends_cap;
     BlkStatus *status;  // per record block
     uint32_t epoch;
-    uint32_t n_blocks;
-    uint32_t blk0;     // first record block of the launch (block b runs as blk0 + b)
+    uint32_t blk0;     // first record block of the launch (ticket k runs block blk0 + k)
     uint64_t wait_ns;  // look-back wait limit
     DevHeader *hdr;
     RowSpec rows;
@@ -65,6 +63,14 @@ struct ColParams {
 // Shared memory of one record block. The tape entries of its records, their
 // separators and the bytes they span are staged with coalesced loads; what
 // does not fit the windows is read from global memory.
+// Record counts of the tape, read on the device from the index pass's
+// header (the host does not wait between the two launches).
+struct TapeCounts {
+    uint64_t n_seps, n_ends;
+    uint64_t n_recs;    // n_ends, plus one for a trailing record without terminator
+    uint32_t n_blocks;  // record blocks
+};
+
 struct ColSmem {
     alignas(16) uint64_t ends[kRecBlock + 2];  // ends[R0 - 2 + i]: 16-byte copies of even pairs
     alignas(16) uint32_t seps[kSepWin + 4];    // seps[sep_lo + i], sep_lo a multiple of 4
@@ -73,6 +79,7 @@ struct ColSmem {
     uint32_t row_base;
     uint32_t arena_base[kMaxStr];
     uint64_t vbits[kMaxCols][kRecWords];
+    uint32_t blk;
     unsigned long long red[kWarps][12];
     alignas(16) uint8_t data[kDataWin + 16];  // 16 bytes of slack for word reads near the window end
 };
@@ -244,44 +251,103 @@ __device__ __forceinline__ void stat_value(StatAcc &a, int k, const Win &W, uint
     else a.inexact[k]++;
 }
 
-// Cleaned bytes of all fields of a record (csv_hash.rs:1207-1230): every
-// byte but the separators and a trailing '\r', less what cleaning removes
-// from fields that open with a quote.
-__device__ __forceinline__ uint32_t record_field_bytes(const Win &W, const Rec &x) {
-    uint32_t tot = (x.end2 - x.start) - (x.nf - 1);
+// A quoted cell s[0, n) (n >= 2, s[0] and s[n-1] are '"') cleaned by the
+// whole warp (csv_hash.rs:1749-1782 append_clean): the inner bytes in
+// chunks of 32, one per lane. Within a run of consecutive quotes the second
+// of each pair is dropped, so a quote is dropped when its position in its
+// run is odd; a run that goes on past a chunk carries its parity. Kept
+// bytes go to dst[at + ...] below cap when dst is given. Returns the
+// cleaned length. Called by all 32 lanes with the same arguments.
+__device__ uint32_t warp_clean(const uint8_t *s, uint32_t n, uint8_t *dst, uint32_t at, uint64_t cap, int lane) {
+    const uint8_t *in = s + 1;
+    const uint32_t il = n - 2;
+    const uint32_t below = (1u << lane) - 1u;
+    uint32_t out = 0, carry = 0;  // cleaned bytes so far; parity of the quote run reaching this chunk
+    for (uint32_t base = 0; base < il; base += 32) {
+        const uint32_t j = base + (uint32_t)lane;
+        const bool inb = j < il;
+        const uint8_t c = inb ? in[j] : (uint8_t)0;
+        const bool isq = inb && c == '"';
+        const uint32_t q = __ballot_sync(0xffffffffu, isq);
+        const uint32_t valid = il - base >= 32 ? 0xffffffffu : (1u << (il - base)) - 1u;
+        const uint32_t nq = ~q & below;  // non-quotes before me in the chunk
+        const uint32_t pos = nq ? (uint32_t)lane - (32u - __clz(nq)) : carry + (uint32_t)lane;
+        const bool drop = isq && (pos & 1u);
+        const uint32_t dm = __ballot_sync(0xffffffffu, drop);
+        const uint32_t keep = valid & ~dm;
+        if (dst && inb && !drop) {
+            const uint64_t o = (uint64_t)at + out + __popc(keep & below);
+            if (o < cap) dst[o] = c;
+        }
+        out += __popc(keep);
+        // the run at the end of the chunk: its parity carries into the next
+        const uint32_t last = 31u - __clz(valid);
+        const uint32_t lastpos = __shfl_sync(0xffffffffu, pos, (int)last);
+        carry = (q >> last) & 1u ? (lastpos + 1u) & 1u : 0u;
+    }
+    return out;
+}
+
+// Cleaned bytes of all fields of the warp's records (csv_hash.rs:1207-1230):
+// every byte but the separators and a trailing '\r', less what cleaning
+// removes from quoted fields; the quoted fields are cleaned by the whole
+// warp. All 32 lanes call it (rows or not).
+__device__ __forceinline__ uint32_t warp_field_bytes(const Win &W, const Rec &x, int lane) {
+    uint32_t tot = x.row ? (x.end2 - x.start) - (x.nf - 1) : 0u;
+    const uint32_t nf = x.row ? x.nf : 0u;
+    uint32_t mx = nf;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
     uint32_t from = x.start;
-    for (uint32_t f = 0; f < x.nf; f++) {
-        const uint32_t to = f + 1 < x.nf ? W.sep(x.sb + f) : x.end2;
-        const uint32_t n = to - from;
-        if (n >= 2 && W.byte(from) == '"') tot -= n - cleaned_len(W.ptr(from, n), n);
-        from = to + 1;
+    for (uint32_t f = 0; f < mx; f++) {
+        bool quoted = false;
+        const uint8_t *src = nullptr;
+        uint32_t n = 0;
+        if (f < nf) {
+            const uint32_t to = f + 1 < nf ? W.sep(x.sb + f) : x.end2;
+            n = to - from;
+            if (n >= 2) {
+                src = W.ptr(from, n);
+                quoted = src[0] == '"' && src[n - 1] == '"';
+            }
+            from = to + 1;
+        }
+        for (uint32_t need = __ballot_sync(0xffffffffu, quoted); need; need &= need - 1) {
+            const int sl = __ffs(need) - 1;
+            const uint8_t *ps = reinterpret_cast<const uint8_t *>(
+                __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(src), sl));
+            const uint32_t ns = __shfl_sync(0xffffffffu, n, sl);
+            const uint32_t cl = warp_clean(ps, ns, nullptr, 0, 0, lane);
+            if (lane == sl) tot -= ns - cl;
+        }
     }
     return tot;
 }
 
 // Record li of the block starting at record R0 (E[li] = ends[R0 + li - 1]).
 template <int D>
-__device__ __forceinline__ Rec make_rec(const ColParams &p, const Win &W, const uint64_t *E, uint64_t R0, int li) {
+__device__ __forceinline__ Rec make_rec(const ColParams &p, const TapeCounts &tc, const Win &W, const uint64_t *E,
+                                        uint64_t R0, int li) {
     Rec x;
     x.row = false;
     x.nf = 0;
     x.start = x.end = x.end2 = x.sb = 0;
     const uint64_t r = R0 + (uint64_t)li;
-    if (r >= p.n_recs) return x;
+    if (r >= tc.n_recs) return x;
     const uint64_t pe = r == 0 ? 0ull : E[li];
     x.start = r == 0 ? 0u : (uint32_t)pe + 1;
     x.sb = r == 0 ? 0u : (uint32_t)(pe >> 32);
     // after the last terminator there is a record only if bytes remain
     // (csv_geo.rs:1094-1100)
-    if (r >= p.n_ends && (uint64_t)x.start >= p.len) return x;
+    if (r >= tc.n_ends && (uint64_t)x.start >= p.len) return x;
     uint32_t se;
-    if (r < p.n_ends) {
+    if (r < tc.n_ends) {
         const uint64_t e = E[li + 1];
         x.end = (uint32_t)e;
         se = (uint32_t)(e >> 32);
     } else {
         x.end = (uint32_t)p.len;
-        se = (uint32_t)p.n_seps;
+        se = (uint32_t)tc.n_seps;
     }
     x.nf = se - x.sb + 1;
     x.row = !(D == D_CSV_HASH && x.start < x.end && W.byte(x.start) == '#');
@@ -293,30 +359,27 @@ __device__ __forceinline__ Rec make_rec(const ColParams &p, const Win &W, const 
 // STATS: the count / sum sink is requested (its code is compiled only
 // into the kernels that need it: a smaller kernel fetches faster).
 template <int D, bool STATS>
-__global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_constant__ ColParams p) {
-    extern __shared__ __align__(16) uint8_t col_smem_raw[];
-    ColSmem &S = *reinterpret_cast<ColSmem *>(col_smem_raw);
+__device__ __forceinline__ void columns_block(const ColParams &p, const TapeCounts &tc, ColSmem &S, uint32_t blk) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const RowSpec &rs = p.rows;
-    const uint32_t blk = p.blk0 + blockIdx.x;
     const uint64_t R0 = (uint64_t)blk * kRecBlock;
     for (int i = tid; i < rs.ncols * kRecWords; i += kThreads) S.vbits[i / kRecWords][i % kRecWords] = 0;
 
     // ---- windows: from the block's first record to its last, computed by
     // every thread from the two tape entries that bound them
-    const uint64_t last = (R0 + kRecBlock < p.n_recs ? R0 + kRecBlock : p.n_recs) - 1;
-    const uint64_t e_first = R0 == 0 ? 0ull : __ldg(reinterpret_cast<const unsigned long long *>(p.ends) + R0 - 1);
-    const uint64_t e_last = last < p.n_ends ? __ldg(reinterpret_cast<const unsigned long long *>(p.ends) + last) : 0ull;
+    const uint64_t last = (R0 + kRecBlock < tc.n_recs ? R0 + kRecBlock : tc.n_recs) - 1;
+    const uint64_t e_first = R0 == 0 ? 0ull : __ldcg(reinterpret_cast<const unsigned long long *>(p.ends) + R0 - 1);
+    const uint64_t e_last = last < tc.n_ends ? __ldcg(reinterpret_cast<const unsigned long long *>(p.ends) + last) : 0ull;
     const bool al16 = ((uintptr_t)p.ends & 15) == 0 && ((uintptr_t)p.seps & 15) == 0;
     const uint64_t sb = R0 == 0 ? 0 : e_first >> 32;
-    const uint64_t se = last < p.n_ends ? e_last >> 32 : p.n_seps;
+    const uint64_t se = last < tc.n_ends ? e_last >> 32 : tc.n_seps;
     const uint64_t sep_lo = al16 ? sb & ~3ull : sb;  // 16-byte aligned start
     const uint32_t sep_n = (uint32_t)(sb - sep_lo) + (uint32_t)(se - sb < (uint64_t)kSepWin ? se - sb : (uint64_t)kSepWin);
     int64_t data_lo;
     uint32_t data_n;
     {
         const int64_t lo = R0 == 0 ? 0 : (int64_t)(uint32_t)e_first + 1;
-        const int64_t hi = last < p.n_ends ? (int64_t)(uint32_t)e_last : (int64_t)p.len;
+        const int64_t hi = last < tc.n_ends ? (int64_t)(uint32_t)e_last : (int64_t)p.len;
         const int64_t q0 = (lo + p.shift) & ~15ll;  // 16-byte aligned address offset
         const int64_t qend = (int64_t)((p.shift + p.len + 15) & ~15ull);
         int64_t qn = ((hi + p.shift + 15) & ~15ll) - q0;
@@ -330,20 +393,20 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
     // in 16-byte pairs from the even index R0 - 2), separators and bytes
     for (int j = tid; j < (kRecBlock + 2) / 2; j += kThreads) {
         const int64_t e0 = (int64_t)R0 - 2 + 2 * j;
-        if (al16 && e0 >= 0 && (uint64_t)e0 + 1 < p.n_ends) {
+        if (al16 && e0 >= 0 && (uint64_t)e0 + 1 < tc.n_ends) {
             cp_async_ca<16>(&S.ends[2 * j], p.ends + e0);
         } else {
-            if (e0 >= 0 && (uint64_t)e0 < p.n_ends) cp_async_ca<8>(&S.ends[2 * j], p.ends + e0);
-            if (e0 + 1 >= 0 && (uint64_t)(e0 + 1) < p.n_ends) cp_async_ca<8>(&S.ends[2 * j + 1], p.ends + e0 + 1);
+            if (e0 >= 0 && (uint64_t)e0 < tc.n_ends) cp_async_ca<8>(&S.ends[2 * j], p.ends + e0);
+            if (e0 + 1 >= 0 && (uint64_t)(e0 + 1) < tc.n_ends) cp_async_ca<8>(&S.ends[2 * j + 1], p.ends + e0 + 1);
         }
     }
     if (al16) {
         for (uint32_t j = tid; 4 * j < sep_n; j += kThreads) {
             const uint64_t i0 = sep_lo + 4 * j;
-            if (i0 + 3 < p.n_seps) {
+            if (i0 + 3 < tc.n_seps) {
                 cp_async_ca<16>(&S.seps[4 * j], p.seps + i0);
             } else {
-                for (uint32_t q = 0; q < 4 && i0 + q < p.n_seps; q++) cp_async_ca<4>(&S.seps[4 * j + q], p.seps + i0 + q);
+                for (uint32_t q = 0; q < 4 && i0 + q < tc.n_seps; q++) cp_async_ca<4>(&S.seps[4 * j + q], p.seps + i0 + q);
             }
         }
     } else {
@@ -364,7 +427,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
     // records
     Rec rec[kRecPerThread];
 #pragma unroll
-    for (int i = 0; i < kRecPerThread; i++) rec[i] = make_rec<D>(p, W, E, R0, warp * 64 + i * 32 + lane);
+    for (int i = 0; i < kRecPerThread; i++) rec[i] = make_rec<D>(p, tc, W, E, R0, warp * 64 + i * 32 + lane);
 
     // ---- per record: row (0/1) and cleaned bytes of each string slot
     const int nv = 1 + rs.nstr;  // values scanned: rows, then string slots
@@ -381,12 +444,24 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
         const uint32_t f = rs.field[c];
 #pragma unroll
         for (int i = 0; i < kRecPerThread; i++) {
-            uint32_t a, b;
+            uint32_t a, b, l = 0;
+            bool quoted = false;
+            const uint8_t *src = nullptr;
             if (rec[i].row && W.field(rec[i], f, a, b)) {
-                const uint32_t l = cleaned_len(W.ptr(a, b - a), b - a);
-#pragma unroll
-                for (int j = 0; j < kMaxStr; j++) v[i][1 + j] += j == k ? l : 0u;
+                l = b - a;
+                src = W.ptr(a, l);
+                quoted = l >= 2 && src[0] == '"' && src[l - 1] == '"';
             }
+            // quoted cells: cleaned length by the whole warp, one cell at a time
+            for (uint32_t need = __ballot_sync(0xffffffffu, quoted); need; need &= need - 1) {
+                const int sl = __ffs(need) - 1;
+                const uint8_t *ps = reinterpret_cast<const uint8_t *>(
+                    __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(src), sl));
+                const uint32_t cl = warp_clean(ps, __shfl_sync(0xffffffffu, l, sl), nullptr, 0, 0, lane);
+                if (lane == sl) l = cl;
+            }
+#pragma unroll
+            for (int j = 0; j < kMaxStr; j++) v[i][1 + j] += j == k ? l : 0u;
         }
     }
 
@@ -495,7 +570,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
             S.row_base = (uint32_t)pre[0];
 #pragma unroll
             for (int k = 0; k < kMaxStr; k++) S.arena_base[k] = (uint32_t)pre[1 + k];  // i32 offsets: checked on the host
-            if (blk == p.n_blocks - 1) {
+            if (blk == tc.n_blocks - 1) {
                 p.hdr->n_rows = pre[0] + tot[0];
 #pragma unroll
                 for (int k = 0; k < kMaxStr; k++) p.hdr->arena[k] = pre[1 + k] + tot[1 + k];
@@ -510,10 +585,11 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
         StatAcc acc = {};
         uint32_t fb_fields = 0, fb_bytes = 0;  // below 2^32: the input is shorter than 4 GiB
         if (rs.want_fb || STATS) {
+            // (the loop is warp-uniform: a warp's lanes take the same number
+            // of records, so the field-byte cleaning can use the whole warp)
             for (int li = tid - 32; li < kRecBlock; li += kThreads - 32) {
-                const Rec x = make_rec<D>(p, W, E, R0, li);
-                if (!x.row) continue;
-                if (STATS) {
+                const Rec x = make_rec<D>(p, tc, W, E, R0, li);
+                if (STATS && x.row) {
                     acc.records++;
 #pragma unroll
                     for (int k = 0; k < 2; k++) {
@@ -522,8 +598,8 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
                     }
                 }
                 if (rs.want_fb) {
-                    fb_fields += x.nf;
-                    fb_bytes += record_field_bytes(W, x);
+                    if (x.row) fb_fields += x.nf;
+                    fb_bytes += warp_field_bytes(W, x, lane);
                 }
             }
         }
@@ -570,6 +646,40 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
 #pragma unroll 1
         for (int i = 0; i < kRecPerThread; i++) {
             const Rec x = i ? rec[1] : rec[0];
+            if (ty == 3) {
+                // strings: every lane takes part (quoted cells are cleaned by
+                // the whole warp after the plain copies)
+                const uint32_t g = i ? grow[1] : grow[0];
+                const uint32_t pos = abase + (i ? pick(ex[1], 1 + k) : pick(ex[0], 1 + k));
+                uint32_t a = 0, b = 0, o;
+                const bool present = x.row && W.field(x, f, a, b);
+                const uint32_t n = b - a;
+                uint8_t *arena = rs.str_data[c];
+                uint32_t len = 0;
+                bool quoted = false;
+                const uint8_t *src = nullptr;
+                if (present) {
+                    src = W.ptr(a, n);
+                    quoted = n >= 2 && src[0] == '"' && src[n - 1] == '"';
+                    if (!quoted) {
+                        if (W.staged(a, n, o) && (uint64_t)pos + n <= rs.str_cap[c]) copy_staged(W.sdata, o, n, arena + pos);
+                        else copy_clean(src, n, arena, pos, rs.str_cap[c]);
+                        len = n;
+                    }
+                }
+                for (uint32_t need = __ballot_sync(0xffffffffu, quoted); need; need &= need - 1) {
+                    const int sl = __ffs(need) - 1;
+                    const uint8_t *ps = reinterpret_cast<const uint8_t *>(
+                        __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(src), sl));
+                    const uint32_t cl = warp_clean(ps, __shfl_sync(0xffffffffu, n, sl), arena,
+                                                   __shfl_sync(0xffffffffu, pos, sl), rs.str_cap[c], lane);
+                    if (lane == sl) len = cl;
+                }
+                if (x.row && g < rs.rows_cap) static_cast<int32_t *>(rs.values[c])[(uint64_t)g + 1] = (int32_t)(pos + len);
+                if (i) okm[1] |= (uint32_t)present << c;
+                else okm[0] |= (uint32_t)present << c;
+                continue;
+            }
             if (!x.row) continue;
             const uint32_t g = i ? grow[1] : grow[0];
             uint32_t a = 0, b = 0, o;
@@ -578,22 +688,7 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
             const bool st = present && W.staged(a, n, o);
             const bool store = g < rs.rows_cap;
             bool ok = present;
-            if (ty == 3) {
-                // arena offset of this record's cell (Arrow i32 offsets: below 2^31)
-                const uint32_t pos = abase + (i ? pick(ex[1], 1 + k) : pick(ex[0], 1 + k));
-                uint32_t len = 0;
-                if (present) {
-                    uint8_t *arena = rs.str_data[c];
-                    if (st && (uint64_t)pos + n <= rs.str_cap[c] &&
-                        !(n >= 2 && W.sdata[o] == '"' && W.sdata[o + n - 1] == '"')) {
-                        copy_staged(W.sdata, o, n, arena + pos);
-                        len = n;
-                    } else {
-                        len = copy_clean(W.ptr(a, n), n, arena, pos, rs.str_cap[c]);
-                    }
-                }
-                if (store) static_cast<int32_t *>(rs.values[c])[(uint64_t)g + 1] = (int32_t)(pos + len);
-            } else if (ty == 1) {
+            if (ty == 1) {
                 uint32_t v = 0;
                 if (present && !(st && swar_u32(W.sdata, o, n, v))) {
                     const Slow64 r = slow_u32(W.ptr(a, n), n);
@@ -685,6 +780,35 @@ __global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_const
             if (tid < 2) atomicAdd(tid == 0 ? &p.hdr->fb_fields : &p.hdr->fb_bytes, t);
             else atomicAdd(&p.hdr->st_records + (tid - 2), t);
         }
+    }
+}
+
+// Persistent launch: CTAs take record blocks from an atomic ticket in the
+// header, so every block before the one a CTA holds has been taken by a
+// running CTA and its look-back always progresses. The record counts come
+// from the index pass's header; a tape larger than the buffers it was
+// written to (the index pass bounds its writes) flags ERR_TAPE and the host
+// runs both passes again with buffers of the exact size.
+template <int D, bool STATS>
+__global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_constant__ ColParams p) {
+    extern __shared__ __align__(16) uint8_t col_smem_raw[];
+    ColSmem &S = *reinterpret_cast<ColSmem *>(col_smem_raw);
+    const int tid = threadIdx.x;
+    TapeCounts tc;
+    tc.n_ends = *(volatile const unsigned long long *)&p.hdr->n_terms;
+    tc.n_seps = *(volatile const unsigned long long *)&p.hdr->n_struct - tc.n_ends;
+    tc.n_recs = tc.n_ends + 1;
+    tc.n_blocks = (uint32_t)((tc.n_recs + kRecBlock - 1) / kRecBlock);
+    if (tc.n_seps > p.seps_cap || tc.n_ends > p.ends_cap) {
+        if (tid == 0 && blockIdx.x == 0) atomicOr(&p.hdr->error, ERR_TAPE);
+        return;
+    }
+    for (;;) {
+        if (tid == 0) S.blk = p.blk0 + atomicAdd(&p.hdr->col_ticket, 1u);
+        __syncthreads();  // also: the previous block is done with shared memory
+        const uint32_t blk = S.blk;
+        if (blk >= tc.n_blocks) break;
+        columns_block<D, STATS>(p, tc, S, blk);
     }
 }
 
