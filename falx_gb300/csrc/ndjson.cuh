@@ -6,8 +6,8 @@
 // inside a string, so every raw '\n' ends a record and tiles need no carried
 // state (the reference's parallel driver snaps chunks to raw newlines the same
 // way, ndjson.rs:857-880). A tile owns the lines that start inside it; each
-// thread parses the lines starting in its 64 bytes, reading the tile from
-// shared memory and the tail of its last line from global memory.
+// thread parses the lines starting in its 64 bytes from shared memory (the
+// tile plus a 4 KiB halo after it).
 //
 // Per record: member "id" of the top-level object must be a JSON integer;
 // member "nested" must be an object whose member "score" is a JSON number
@@ -161,35 +161,89 @@ __device__ inline bool j_dec_e6(const LineView &v, int64_t e, int64_t i, int64_t
     return true;
 }
 
-constexpr int kNdTile = 16384;
+constexpr int kNdTile = 16384;  // a tile owns the lines that start inside it
+constexpr int kNdHalo = 4096;   // bytes staged after the tile for the lines that cross its end
+constexpr int kNdSpan = kNdTile + kNdHalo;
+constexpr int kNdWords = kNdSpan / 64;
 
+struct NdSmem {
+    alignas(16) uint8_t buf[16 + kNdSpan];  // 16 bytes before the tile, the tile, the halo
+    uint64_t nl[kNdWords];                  // newline bitmap of the tile and the halo
+    unsigned long long red[kWarps][5];
+    uint32_t s_tile;
+};
+
+// Tiles sit on the 16-byte address grid of the input: tile t starts at file
+// position kNdTile t - shift, so every staging load is an aligned 16-byte
+// load. A thread finds the line starts among its 64 bytes of the tile from
+// the newline bitmap, the end of each line from the bitmap too (lines
+// crossing into the halo included), and parses each line from shared
+// memory; only a line longer than the halo reads global memory past it.
 __global__ void __launch_bounds__(kThreads) ndjson_kernel(const uint8_t *data, uint64_t len, uint32_t ntiles,
                                                            NdjsonAcc *acc) {
-    __shared__ __align__(16) uint8_t sm[kNdTile + 16];
-    __shared__ unsigned long long red[kWarps][5];
-    __shared__ uint32_t s_tile;
+    __shared__ NdSmem S;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t shift = (uint32_t)((uintptr_t)data & 15u);
+    const uint8_t *abase = data - shift;
+    const uint64_t end16 = (shift + len + 15) & ~15ull;  // staged bytes stay inside [abase, abase + end16)
     for (;;) {
-        if (tid == 0) s_tile = atomicAdd(&acc->ticket, 1u);
+        if (tid == 0) S.s_tile = atomicAdd(&acc->ticket, 1u);
         __syncthreads();
-        const uint32_t tile = s_tile;
+        const uint32_t tile = S.s_tile;
         if (tile >= ntiles) break;
-        const int64_t t0 = (int64_t)tile * kNdTile;
-        const int64_t t1 = t0 + kNdTile < (int64_t)len ? t0 + kNdTile : (int64_t)len;
-        // stage [t0 - 1, t1): one byte before the tile for the line-start test
-        const int64_t s0 = t0 > 0 ? t0 - 1 : 0;
-        for (int64_t i = s0 + tid; i < t1; i += kThreads) sm[i - s0] = data[i];
+        const uint64_t a0 = (uint64_t)tile * kNdTile;     // address offset of the tile
+        const int64_t t0 = (int64_t)a0 - (int64_t)shift;  // its file position
+        // ---- stage [a0 - 16, a0 + kNdSpan) with aligned 16-byte loads
+        for (int i = tid; i < (16 + kNdSpan) / 16; i += kThreads) {
+            const int64_t o = (int64_t)a0 - 16 + 16 * i;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (o >= 0 && (uint64_t)o < end16) v = *reinterpret_cast<const uint4 *>(abase + o);
+            *reinterpret_cast<uint4 *>(S.buf + 16 * i) = v;
+        }
         __syncthreads();
-        LineView v{sm, s0, t1, data};
+        // ---- newline bitmap (positions outside the input are not newlines)
+        for (int k = tid; k < kNdWords; k += kThreads) {
+            const uint32_t *w = reinterpret_cast<const uint32_t *>(S.buf + 16 + 64 * k);
+            uint64_t m = 0;
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                m |= (uint64_t)gather16(eq_flags(w[4 * c], '\n'), eq_flags(w[4 * c + 1], '\n'),
+                                        eq_flags(w[4 * c + 2], '\n'), eq_flags(w[4 * c + 3], '\n'))
+                     << (16 * c);
+            const int64_t p0 = t0 + 64 * k;
+            if (p0 < 0) m &= p0 <= -64 ? 0ull : ~0ull << (-p0);
+            if (p0 + 64 > (int64_t)len) m &= p0 >= (int64_t)len ? 0ull : (1ull << ((int64_t)len - p0)) - 1;
+            S.nl[k] = m;
+        }
+        __syncthreads();
+        LineView v{S.buf + 16, t0, t0 + kNdSpan, data};
         unsigned long long recs = 0, sid = 0, ssc = 0;
         __int128 tot = 0;
         bool bad = false;
-        const int64_t b0 = t0 + (int64_t)tid * kThreadBytes;
-        const int64_t b1 = b0 + kThreadBytes < t1 ? b0 + kThreadBytes : t1;
-        for (int64_t p = b0; p < b1; p++) {
-            if (!(p == 0 || v.at(p - 1) == '\n')) continue;
-            int64_t e = p;
-            while (e < (int64_t)len && v.at(e) != '\n') e++;
+        // line starts among this thread's 64 bytes of the tile
+        const int64_t b0 = t0 + 64 * tid;
+        uint64_t starts = S.nl[tid] << 1;
+        if (tid > 0) starts |= S.nl[tid - 1] >> 63;
+        else if (b0 > 0 && S.buf[15] == '\n') starts |= 1;
+        if (b0 <= 0 && b0 + 64 > 0) starts |= 1ull << (-b0);  // file position 0
+        if (b0 < 0) starts &= b0 <= -64 ? 0ull : ~0ull << (-b0);
+        if (b0 + 64 > (int64_t)len) starts &= b0 >= (int64_t)len ? 0ull : (1ull << ((int64_t)len - b0)) - 1;
+        while (starts) {
+            const int bpos = __ffsll((long long)starts) - 1;
+            starts &= starts - 1;
+            const int64_t p = b0 + bpos;
+            // end of the line: the next newline in the bitmap, else past the halo
+            int wi = tid;
+            uint64_t m = S.nl[wi] & (~0ull << bpos);
+            while (!m && wi + 1 < kNdWords) m = S.nl[++wi];
+            int64_t e;
+            if (m) {
+                e = t0 + 64 * wi + (__ffsll((long long)m) - 1);
+            } else {
+                e = t0 + kNdSpan;
+                while (e < (int64_t)len && data[e] != '\n') e++;
+                if (e > (int64_t)len) e = (int64_t)len;
+            }
             int64_t j = p;
             j_ws(v, e, j);
             if (j >= e) continue;
@@ -218,14 +272,14 @@ __global__ void __launch_bounds__(kThreads) ndjson_kernel(const uint8_t *data, u
             for (int k = 0; k < 3; k++) vals[k] += __shfl_down_sync(0xffffffffu, vals[k], d);
         }
         if (lane == 0)
-            for (int k = 0; k < 5; k++) red[warp][k] = vals[k];
+            for (int k = 0; k < 5; k++) S.red[warp][k] = vals[k];
         if (__syncthreads_or(bad) && tid == 0) atomicOr(&acc->error, 1u);
         if (tid == 0) {
             unsigned long long r[5] = {0, 0, 0, 0, 0};
             for (int w = 0; w < kWarps; w++) {
-                for (int k = 0; k < 3; k++) r[k] += red[w][k];
-                unsigned long long nlo = r[3] + red[w][3];
-                r[4] += red[w][4] + (nlo < r[3] ? 1 : 0);
+                for (int k = 0; k < 3; k++) r[k] += S.red[w][k];
+                unsigned long long nlo = r[3] + S.red[w][3];
+                r[4] += S.red[w][4] + (nlo < r[3] ? 1 : 0);
                 r[3] = nlo;
             }
             atomicAdd(&acc->records, r[0]);
@@ -251,7 +305,8 @@ inline int ndjson_run(const uint8_t *data, uint64_t len, falx_ndjson_stats *out,
                       cudaStream_t stream) {
     memset(out, 0, sizeof *out);
     if (len == 0) return FALX_OK;
-    uint32_t ntiles = (uint32_t)((len + kNdTile - 1) / kNdTile);
+    const uint64_t shift = (uint64_t)((uintptr_t)data & 15u);
+    uint32_t ntiles = (uint32_t)((len + shift + kNdTile - 1) / kNdTile);
     uint32_t grid = (uint32_t)(g_nd_sm_count * 4);
     if (grid > ntiles) grid = ntiles;
     if (cudaMemsetAsync(acc, 0, sizeof(NdjsonAcc), stream) != cudaSuccess) return FALX_ERR_CUDA;
