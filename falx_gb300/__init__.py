@@ -10,6 +10,7 @@ ndjson.rs) with the dialect as an argument:
         Parsed.records() -> Record.fields()    csv_geo.rs:424-686
     parse_columns(data, schema) -> Columns     csv_geo.rs:1112  (and _par :1216, _chunks_par :1167)
     parse_csv_geo_stats(data, ...)             csv_geo.rs:1505  (and _par, :1513)
+    parse_csv_geo_text_stats(data, ...)        csv_geo_text.rs:1627  (and _par, :1637)
     parse_field_bytes(data, dialect)           csv_hash.rs:976  (and _par, :984)
     parse_ndjson_id_score(data)                ndjson.rs:679    (and _par, :726)
     bitmap_get, string_at                      csv_geo.rs:1105, csv_hash.rs:1444
@@ -33,7 +34,7 @@ __all__ = [
     "CSV", "CSV_HASH", "TSV", "LOGFMT", "NDJSON", "I64", "U32", "F64", "STR", "BYTES", "FalxError",
     "Engine", "Schema", "Columns", "Parsed", "Record", "index_structurals", "index_structurals_par", "parse",
     "parse_par", "parse_columns", "parse_columns_par", "parse_columns_chunks_par", "parse_csv_geo_stats",
-    "parse_csv_geo_stats_par", "parse_field_bytes", "parse_field_bytes_par", "parse_ndjson_id_score",
+    "parse_csv_geo_stats_par", "parse_csv_geo_text_stats", "parse_csv_geo_text_stats_par", "parse_field_bytes", "parse_field_bytes_par", "parse_ndjson_id_score",
     "parse_ndjson_id_score_par", "bitmap_get", "string_at", "engine",
 ]
 
@@ -294,6 +295,17 @@ class Engine:
         check(self.lib.falx_stats_count_sum(self.ctx, dialect, c_void_p(d.data_ptr()), d.numel(), field0, field1,
                                             byref(st)), "falx_stats_count_sum")
         return GeoStats(st)
+
+    def geo_text_stats(self, data, dialect=CSV, fields=(1, 4, 5)):
+        """City text lane plus lat / lon counts and checksums
+        (csv_geo_text.rs:1627 parse_csv_geo_text_stats); fields = (city,
+        latitude, longitude) ordinals."""
+        d = self.to_device(data)
+        self._sync_stream()
+        st = _lib.falx_geo_text_stats()
+        check(self.lib.falx_csv_geo_text_stats(self.ctx, dialect, c_void_p(d.data_ptr()), d.numel(), fields[0],
+                                               fields[1], fields[2], byref(st)), "falx_csv_geo_text_stats")
+        return st
 
     def field_bytes(self, data, dialect):
         d = self.to_device(data)
@@ -649,6 +661,14 @@ def parse_csv_geo_stats(data, dialect=CSV, fields=(4, 5)):
 
 def parse_csv_geo_stats_par(data, threads=1, dialect=CSV, fields=(4, 5)):
     return parse_csv_geo_stats(data, dialect, fields)
+
+
+def parse_csv_geo_text_stats(data, dialect=CSV, fields=(1, 4, 5)):
+    return engine().geo_text_stats(data, dialect, fields)
+
+
+def parse_csv_geo_text_stats_par(data, threads=1, dialect=CSV, fields=(1, 4, 5)):
+    return parse_csv_geo_text_stats(data, dialect, fields)
 
 
 def parse_field_bytes(data, dialect=CSV_HASH):

@@ -44,6 +44,12 @@ class falx_geo_stats(Structure):
                 ("sum_e6", c_int64 * 2), ("inexact", c_uint64 * 2), ("sum_f64", c_double * 2)]
 
 
+class falx_geo_text_stats(Structure):
+    _fields_ = [("records", c_uint64), ("city_values", c_uint64), ("city_bytes", c_uint64),
+                ("city_checksum", c_uint64), ("latitude_values", c_uint64), ("longitude_values", c_uint64),
+                ("latitude_checksum", c_uint64), ("longitude_checksum", c_uint64)]
+
+
 class falx_field_byte_stats(Structure):
     _fields_ = [("fields", c_uint64), ("bytes", c_uint64)]
 
@@ -98,6 +104,8 @@ SIGNATURES = {
     "falx_stats_count_sum": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_uint32, c_uint32,
                                      POINTER(falx_geo_stats)]),
     "falx_field_bytes": (c_int, [c_void_p, c_int, c_void_p, c_uint64, POINTER(falx_field_byte_stats)]),
+    "falx_csv_geo_text_stats": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_uint32, c_uint32, c_uint32,
+                                        POINTER(falx_geo_text_stats)]),
     "falx_parse": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, POINTER(falx_outputs)]),
     "falx_ndjson_id_score": (c_int, [c_void_p, c_void_p, c_uint64, POINTER(falx_ndjson_stats)]),
     "falx_index_structurals_host": (c_int, [c_void_p, c_int, c_void_p, c_uint64, c_void_p, c_uint64,

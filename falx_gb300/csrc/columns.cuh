@@ -80,7 +80,7 @@ struct ColSmem {
     uint32_t arena_base[kMaxStr];
     uint64_t vbits[kMaxCols][kRecWords];
     uint32_t blk;
-    unsigned long long red[kWarps][12];
+    unsigned long long red[kWarps][14];
     alignas(16) uint8_t data[kDataWin + 16];  // 16 bytes of slack for word reads near the window end
 };
 
@@ -257,8 +257,10 @@ __device__ __forceinline__ void stat_value(StatAcc &a, int k, const Win &W, uint
 // of each pair is dropped, so a quote is dropped when its position in its
 // run is odd; a run that goes on past a chunk carries its parity. Kept
 // bytes go to dst[at + ...] below cap when dst is given. Returns the
-// cleaned length. Called by all 32 lanes with the same arguments.
-__device__ uint32_t warp_clean(const uint8_t *s, uint32_t n, uint8_t *dst, uint32_t at, uint64_t cap, int lane) {
+// cleaned length; `sum`, when given, gets the sum of the kept byte values
+// added. Called by all 32 lanes with the same arguments.
+__device__ uint32_t warp_clean(const uint8_t *s, uint32_t n, uint8_t *dst, uint32_t at, uint64_t cap, int lane,
+                               uint64_t *sum = nullptr) {
     const uint8_t *in = s + 1;
     const uint32_t il = n - 2;
     const uint32_t below = (1u << lane) - 1u;
@@ -280,12 +282,51 @@ __device__ uint32_t warp_clean(const uint8_t *s, uint32_t n, uint8_t *dst, uint3
             if (o < cap) dst[o] = c;
         }
         out += __popc(keep);
+        if (sum) *sum += __reduce_add_sync(0xffffffffu, inb && !drop ? (uint32_t)c : 0u);
         // the run at the end of the chunk: its parity carries into the next
         const uint32_t last = 31u - __clz(valid);
         const uint32_t lastpos = __shfl_sync(0xffffffffu, pos, (int)last);
         carry = (q >> last) & 1u ? (lastpos + 1u) & 1u : 0u;
     }
     return out;
+}
+
+// Sum of the byte values of p[0, n) (any alignment; shared or global).
+__device__ __forceinline__ uint32_t byte_sum(const uint8_t *p, uint32_t n) {
+    uint32_t s = 0, i = 0;
+    while (i < n && ((uintptr_t)(p + i) & 3u)) s += p[i++];
+    for (; i + 4 <= n; i += 4) s = __dp4a(*reinterpret_cast<const uint32_t *>(p + i), 0x01010101u, s);
+    while (i < n) s += p[i++];
+    return s;
+}
+
+// City text lane of the warp's records (csv_geo_text.rs:1845-1937): per row
+// whose city field is present, one value, its cleaned length and the sum of
+// its cleaned byte values; quoted cells are cleaned by the whole warp. All
+// 32 lanes call it.
+__device__ __forceinline__ void warp_text_cell(const Win &W, const Rec &x, uint32_t f, int lane, uint64_t &values,
+                                               uint64_t &bytes, uint64_t &checksum) {
+    uint32_t a = 0, b = 0;
+    const bool present = x.row && W.field(x, f, a, b);
+    const uint32_t n = b - a;
+    const uint8_t *src = present ? W.ptr(a, n) : nullptr;
+    const bool quoted = present && n >= 2 && src[0] == '"' && src[n - 1] == '"';
+    if (present) values++;
+    if (present && !quoted) {
+        bytes += n;
+        checksum += byte_sum(src, n);
+    }
+    for (uint32_t need = __ballot_sync(0xffffffffu, quoted); need; need &= need - 1) {
+        const int sl = __ffs(need) - 1;
+        const uint8_t *ps = reinterpret_cast<const uint8_t *>(
+            __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(src), sl));
+        uint64_t sum = 0;
+        const uint32_t cl = warp_clean(ps, __shfl_sync(0xffffffffu, n, sl), nullptr, 0, 0, lane, &sum);
+        if (lane == sl) {
+            bytes += cl;
+            checksum += sum;
+        }
+    }
 }
 
 // Cleaned bytes of all fields of the warp's records (csv_hash.rs:1207-1230):
@@ -577,13 +618,14 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
             }
         }
         if (lane == 0)
-            for (int k = 0; k < 11; k++) S.red[0][k] = 0;
+            for (int k = 0; k < 14; k++) S.red[0][k] = 0;
     } else {
         // ---- meanwhile warps 1-7: field-byte and count / sum totals of all
         // the block's records (they need no prefix), warp sums into shared
         // memory for the block totals at the end
         StatAcc acc = {};
         uint32_t fb_fields = 0, fb_bytes = 0;  // below 2^32: the input is shorter than 4 GiB
+        uint64_t tx_values = 0, tx_bytes = 0, tx_sum = 0;
         if (rs.want_fb || STATS) {
             // (the loop is warp-uniform: a warp's lanes take the same number
             // of records, so the field-byte cleaning can use the whole warp)
@@ -601,10 +643,12 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
                     if (x.row) fb_fields += x.nf;
                     fb_bytes += warp_field_bytes(W, x, lane);
                 }
+                if (STATS && rs.want_text) warp_text_cell(W, x, rs.text_field, lane, tx_values, tx_bytes, tx_sum);
             }
         }
-        unsigned long long r[11] = {fb_fields, fb_bytes, acc.records, acc.values[0], acc.values[1], acc.checksum[0],
-                                    acc.checksum[1], acc.sum_e6[0], acc.sum_e6[1], acc.inexact[0], acc.inexact[1]};
+        unsigned long long r[14] = {fb_fields,      fb_bytes,       acc.records,    acc.values[0], acc.values[1],
+                                    acc.checksum[0], acc.checksum[1], acc.sum_e6[0],  acc.sum_e6[1], acc.inexact[0],
+                                    acc.inexact[1],  tx_values,       tx_bytes,       tx_sum};
         if (!STATS) {
             uint32_t f = fb_fields, by = fb_bytes;
 #pragma unroll
@@ -616,16 +660,16 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
             r[1] = by;
         } else {
 #pragma unroll
-            for (int k = 0; k < 11; k++) {
+            for (int k = 0; k < 14; k++) {
 #pragma unroll
                 for (int d = 16; d > 0; d >>= 1) r[k] += __shfl_down_sync(0xffffffffu, r[k], d);
             }
         }
         if (lane == 0)
-            for (int k = 0; k < 11; k++) S.red[warp][k] = r[k];
+            for (int k = 0; k < 14; k++) S.red[warp][k] = r[k];
     }
     __syncthreads();
-    const int nred = STATS ? 11 : rs.want_fb ? 2 : 0;
+    const int nred = STATS ? 14 : rs.want_fb ? 2 : 0;  // block totals: st_records .. st_text[2] follow fb
 
     // ---- cells, column by column
     const uint32_t row_base = S.row_base;

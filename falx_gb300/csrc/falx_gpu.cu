@@ -876,7 +876,10 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     return FALX_OK;
 }
 
-int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, uint64_t len, falx_outputs *o) {
+// text_field: the City text lane's field (with o->stats: lat / lon), or
+// negative for none.
+int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, uint64_t len, falx_outputs *o,
+                 int64_t text_field = -1) {
     if (!schema || !o) return FALX_ERR_INVALID;
     int dialect = schema->dialect;
     int rc = check_common(c, dialect, data, len);
@@ -914,6 +917,9 @@ int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, ui
         uint32_t mf = (o->stats_fields[0] > o->stats_fields[1] ? o->stats_fields[0] : o->stats_fields[1]) + 1;
         if (mf > rs.max_field) rs.max_field = mf;
     }
+    rs.want_text = text_field >= 0 && rs.want_stats;
+    rs.text_field = rs.want_text ? (uint32_t)text_field : 0u;
+    if (rs.want_text && rs.text_field + 1 > rs.max_field) rs.max_field = rs.text_field + 1;
     o->n_index = o->n_seps = o->n_ends = 0;
     if (o->columns) o->columns->rows = 0;
     if (len == 0) {
@@ -929,7 +935,7 @@ int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, ui
         if (o->stats) memset(o->stats, 0, sizeof *o->stats);
         return FALX_OK;
     }
-    if (rows && c->rows_path == 0) rc = rows_two_pass(c, dialect, data, len, P);
+    if (rows && (c->rows_path == 0 || rs.want_text)) rc = rows_two_pass(c, dialect, data, len, P);
     else rc = run_scan(c, dialect, rows, data, len, P);
     if (rc && rc != FALX_ERR_CAPACITY) return rc;  // on CAPACITY the counts are still reported
     const DevHeader &h = *c->hhdr;
@@ -1142,6 +1148,32 @@ int falx_stats_count_sum(falx_ctx *c, int dialect, const uint8_t *data, uint64_t
     o.stats_fields[0] = field0;
     o.stats_fields[1] = field1;
     return parse_device(c, &s, data, len, &o);
+}
+
+int falx_csv_geo_text_stats(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, uint32_t city_field,
+                            uint32_t lat_field, uint32_t lon_field, falx_geo_text_stats *out) {
+    if (!out || dialect == FALX_NDJSON) return FALX_ERR_INVALID;
+    falx_schema s;
+    memset(&s, 0, sizeof s);
+    s.dialect = dialect;
+    falx_geo_stats st;
+    falx_outputs o;
+    memset(&o, 0, sizeof o);
+    o.stats = &st;
+    o.stats_fields[0] = lat_field;
+    o.stats_fields[1] = lon_field;
+    memset(out, 0, sizeof *out);
+    const int rc = parse_device(c, &s, data, len, &o, (int64_t)city_field);
+    if (rc) return rc;
+    out->records = st.records;
+    out->city_values = len ? c->hhdr->st_text[0] : 0;
+    out->city_bytes = len ? c->hhdr->st_text[1] : 0;
+    out->city_checksum = len ? c->hhdr->st_text[2] : 0;
+    out->latitude_values = st.values[0];
+    out->longitude_values = st.values[1];
+    out->latitude_checksum = st.checksum[0];
+    out->longitude_checksum = st.checksum[1];
+    return FALX_OK;
 }
 
 int falx_field_bytes(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, falx_field_byte_stats *out) {

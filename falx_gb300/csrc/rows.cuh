@@ -40,6 +40,8 @@ struct RowSpec {
     int want_fb;
     int want_stats;
     uint32_t stats_field[2];
+    int want_text;        // City text lane (with want_stats): values, cleaned bytes, byte checksum
+    uint32_t text_field;
 };
 
 template <bool ROWS>

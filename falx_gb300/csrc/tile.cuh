@@ -46,6 +46,7 @@ struct DevHeader {
     unsigned long long arena[kMaxStr];
     unsigned long long fb_fields, fb_bytes;
     unsigned long long st_records, st_values[2], st_checksum[2], st_sum_e6[2], st_inexact[2];
+    unsigned long long st_text[3];  // City text lane: values, cleaned bytes, wrapping byte checksum
     unsigned long long spec_repairs;  // speculative tiles whose assumed entry state was wrong
     uint32_t col_ticket;              // record blocks taken by the columns pass
     uint32_t pad2;

@@ -153,6 +153,24 @@ int falx_stats_count_sum(falx_ctx *ctx, int dialect, const uint8_t *data, uint64
                          uint32_t field1, falx_geo_stats *out);
 
 typedef struct {
+    uint64_t records;
+    uint64_t city_values;        /* rows whose city field is present */
+    uint64_t city_bytes;         /* cleaned bytes of those cells */
+    uint64_t city_checksum;      /* wrapping sum of their cleaned byte values */
+    uint64_t latitude_values;
+    uint64_t longitude_values;
+    uint64_t latitude_checksum;  /* wrapping sum of f64 bit patterns */
+    uint64_t longitude_checksum;
+} falx_geo_text_stats;
+
+/* City text lane with the lat / lon count and checksums, without
+ * materialising columns. Replaces parse_csv_geo_text_stats /
+ * parse_csv_geo_text_stats_par (csv_geo_text.rs:1627, :1637; sink
+ * :1845-1937). csv_hash comment records are not rows. */
+int falx_csv_geo_text_stats(falx_ctx *ctx, int dialect, const uint8_t *data, uint64_t len, uint32_t city_field,
+                            uint32_t lat_field, uint32_t lon_field, falx_geo_text_stats *out);
+
+typedef struct {
     uint64_t fields;
     uint64_t bytes;
 } falx_field_byte_stats;

@@ -29,6 +29,11 @@ class orc_geo_stats(Structure):
                 ("sum_e6", c_int64 * 2), ("inexact", c_uint64 * 2), ("fold", c_double * 2)]
 
 
+class orc_text_stats(Structure):
+    _fields_ = [("records", c_uint64), ("city_values", c_uint64), ("city_bytes", c_uint64),
+                ("city_checksum", c_uint64), ("values", c_uint64 * 2), ("checksum", c_uint64 * 2)]
+
+
 class orc_ndjson_stats(Structure):
     _fields_ = [("records", c_uint64), ("sum_id", c_int64), ("sum_score_e6", c_int64), ("total_e6_lo", c_int64),
                 ("total_e6_hi", c_int64), ("total_f64", c_double)]
@@ -81,6 +86,9 @@ def lib():
         l.orc_par_ndjson_json.argtypes = [c_void_p, c_uint64, c_int, POINTER(orc_ndjson_stats)]
         l.orc_par_geo_stats.restype = None
         l.orc_par_geo_stats.argtypes = [c_int, c_void_p, c_uint64, c_int, c_uint32, c_uint32, POINTER(orc_geo_stats)]
+        l.orc_geo_text_stats.restype = None
+        l.orc_geo_text_stats.argtypes = [c_int, c_void_p, c_uint64, c_uint32, c_uint32, c_uint32,
+                                         POINTER(orc_text_stats)]
         l.falx_gen.restype = c_uint64
         l.falx_gen.argtypes = [c_int, c_uint64, c_uint64, c_void_p, c_uint64, c_int]
         l.orc_par_field_bytes.restype = None
@@ -235,6 +243,13 @@ def geo_stats_par(data, dialect, f0, f1, threads):
     a, p, n = _buf(data)
     st = orc_geo_stats()
     lib().orc_par_geo_stats(dialect, p, n, threads, f0, f1, byref(st))
+    return st
+
+
+def geo_text_stats(data, dialect, city, lat, lon):
+    a, p, n = _buf(data)
+    st = orc_text_stats()
+    lib().orc_geo_text_stats(dialect, p, n, city, lat, lon, byref(st))
     return st
 
 

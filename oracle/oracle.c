@@ -696,6 +696,61 @@ void orc_geo_stats_run(int dialect, const uint8_t *d, uint64_t n, uint32_t field
     free(c.scratch);
 }
 
+/* --------------------------- City text lane ------------------------------ */
+/* CsvGeoTextStats (csv_geo_text.rs:1845-1937): per record, the city cell's
+ * presence, cleaned length and the wrapping sum of its cleaned byte values;
+ * the lat / lon cells' values and wrapping sums of their f64 bit patterns
+ * (numeric cells cleaned first when they open with a quote). */
+typedef struct {
+    int dialect;
+    uint32_t f[3];
+    orc_text_stats *st;
+} text_ctx;
+
+static void text_record(void *vctx, const uint8_t *d, const orc_record *r) {
+    text_ctx *c = (text_ctx *)vctx;
+    if (is_comment(c->dialect, d, r)) return;
+    c->st->records++;
+    if (c->f[0] < r->nfields) {
+        const uint8_t *raw = d + r->fstart[c->f[0]];
+        const uint64_t len = r->fend[c->f[0]] - r->fstart[c->f[0]];
+        uint64_t bytes = 0, sum = 0;
+        if (len >= 2 && raw[0] == '"' && raw[len - 1] == '"') {
+            const uint8_t *in = raw + 1;
+            const uint64_t il = len - 2;
+            uint64_t i = 0;
+            while (i < il) {
+                bytes++;
+                sum += in[i];
+                i += (in[i] == '"' && i + 1 < il && in[i + 1] == '"') ? 2 : 1;
+            }
+        } else {
+            bytes = len;
+            for (uint64_t i = 0; i < len; i++) sum += raw[i];
+        }
+        c->st->city_values++;
+        c->st->city_bytes += bytes;
+        c->st->city_checksum += sum;
+    }
+    for (int k = 0; k < 2; k++) {
+        const uint32_t f = c->f[1 + k];
+        if (f >= r->nfields) continue;
+        uint64_t bits;
+        int64_t e6;
+        int exact;
+        if (!orc_stats_cell(d + r->fstart[f], r->fend[f] - r->fstart[f], &bits, &e6, &exact)) continue;
+        c->st->values[k]++;
+        c->st->checksum[k] += bits;
+    }
+}
+
+void orc_geo_text_stats(int dialect, const uint8_t *d, uint64_t n, uint32_t city, uint32_t lat, uint32_t lon,
+                        orc_text_stats *out) {
+    memset(out, 0, sizeof *out);
+    text_ctx c = {dialect, {city, lat, lon}, out};
+    walk_records(dialect, d, n, text_record, &c);
+}
+
 /* --------------------------- field bytes --------------------------------- */
 
 typedef struct {

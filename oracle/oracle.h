@@ -107,6 +107,16 @@ int orc_parse_f64(const uint8_t *s, uint64_t len, double *out);
 int orc_parse_i64(const uint8_t *s, uint64_t len, int64_t *out);
 int orc_parse_u32(const uint8_t *s, uint64_t len, uint32_t *out);
 
+/* City text lane (csv_geo_text.rs:1607-1640 CsvGeoTextStats). */
+typedef struct {
+    uint64_t records;
+    uint64_t city_values, city_bytes, city_checksum; /* checksum: wrapping sum of cleaned byte values */
+    uint64_t values[2];                             /* latitude, longitude */
+    uint64_t checksum[2];                           /* wrapping sums of their f64 bit patterns */
+} orc_text_stats;
+void orc_geo_text_stats(int dialect, const uint8_t *d, uint64_t n, uint32_t city, uint32_t lat, uint32_t lon,
+                        orc_text_stats *out);
+
 /* Multi-threaded port of the reference's `_par` drivers, used as the timed
  * CPU baseline (csv_hash.rs:345-399 three-phase index, :1507-1601 columns,
  * :984-1051 field bytes; csv_geo.rs:1513-1561 stats; ndjson.rs:726-750). */
