@@ -6,7 +6,7 @@ src/kernels/csv_geo.rs, csv_hash.rs, csv_typed.rs, tsv.rs, logfmt.rs,
 ndjson.rs) with the dialect as an argument:
 
     index_structurals(data, dialect)           csv_geo.rs:24    (and _par, :95)
-    parse(data, dialect) -> Parsed             csv_geo.rs:394   (and parse_par, :215)
+    parse(data, dialect) -> Parsed             csv_geo.rs:394   (and parse_par, :215; parse_into, :405)
         Parsed.records() -> Record.fields()    csv_geo.rs:424-686
     parse_columns(data, schema) -> Columns     csv_geo.rs:1112  (and _par :1216, _chunks_par :1167)
     parse_csv_geo_stats(data, ...)             csv_geo.rs:1505  (and _par, :1513)
@@ -33,7 +33,7 @@ from ._lib import BYTES, CSV, CSV_HASH, F64, I64, LOGFMT, NDJSON, STR, TSV, U32,
 __all__ = [
     "CSV", "CSV_HASH", "TSV", "LOGFMT", "NDJSON", "I64", "U32", "F64", "STR", "BYTES", "FalxError",
     "Engine", "Schema", "Columns", "Parsed", "Record", "index_structurals", "index_structurals_par", "parse",
-    "parse_par", "parse_columns", "parse_columns_par", "parse_columns_chunks_par", "parse_csv_geo_stats",
+    "parse_par", "parse_into", "parse_columns", "parse_columns_par", "parse_columns_chunks_par", "parse_csv_geo_stats",
     "parse_csv_geo_stats_par", "parse_csv_geo_text_stats", "parse_csv_geo_text_stats_par", "parse_field_bytes", "parse_field_bytes_par", "parse_ndjson_id_score",
     "parse_ndjson_id_score_par", "bitmap_get", "string_at", "engine",
 ]
@@ -127,15 +127,22 @@ class Engine:
             check(rc, "falx_index_structurals")
             return out[: cnt.value]
 
-    def parse_tape(self, data, dialect=CSV):
-        """(seps int32 tensor, ends int64 tensor) of the record tape."""
+    def parse_tape(self, data, dialect=CSV, reuse=None):
+        """(seps int32 tensor, ends int64 tensor) of the record tape. `reuse`:
+        (seps, ends) device tensors of an earlier tape to write into when
+        they are large enough."""
         d = self.to_device(data)
         n = d.numel()
         self._sync_stream()
         scap, ecap = n // 4 + 1024, n // 16 + 1024
+        if reuse is not None:
+            scap, ecap = max(scap, reuse[0].numel()), max(ecap, reuse[1].numel())
         while True:
-            seps = self.empty(scap, self.torch.int32)
-            ends = self.empty(ecap, self.torch.int64)
+            if reuse is not None and reuse[0].numel() >= scap and reuse[1].numel() >= ecap:
+                seps, ends = reuse
+            else:
+                seps = self.empty(scap, self.torch.int32)
+                ends = self.empty(ecap, self.torch.int64)
             ns, ne = c_uint64(), c_uint64()
             rc = self.lib.falx_parse_tape(self.ctx, dialect, c_void_p(d.data_ptr()), n, c_void_p(seps.data_ptr()),
                                           scap, c_void_p(ends.data_ptr()), ecap, byref(ns), byref(ne))
@@ -641,6 +648,18 @@ def parse(data, dialect=CSV):
 
 def parse_par(data, threads=1, dialect=CSV):
     return parse(data, dialect)
+
+
+def parse_into(data, recycle, dialect=CSV):
+    """Like parse, writing the tape into the device buffers of an earlier
+    Parsed (csv_geo.rs:405 parse_into: the tape allocations are recycled,
+    their contents discarded)."""
+    reuse = getattr(recycle, "_device", None) if recycle is not None else None
+    seps, ends = engine().parse_tape(data, dialect, reuse=reuse)
+    p = Parsed(_host_bytes(data), seps.cpu().numpy().view(np.uint32), ends.cpu().numpy().view(np.uint64), dialect)
+    # keep the whole device buffers (the tape tensors are views of them) for the next recycle
+    p._device = tuple(t._base if t._base is not None else t for t in (seps, ends))
+    return p
 
 
 def parse_columns(data, schema):
