@@ -1241,7 +1241,9 @@ typedef int (*WriteValue32Fn)(void *stream, unsigned long long addr, unsigned in
 // Copy host_data into c->dev_in as chunks on the copy stream, each followed
 // by a flag write (cuStreamWriteValue32: the driver fences the copy before
 // the write). Returns 1 when the chunks are queued and the first index
-// launch should wait on them, 0 when the caller should copy as usual.
+// launch should wait on them, 2 when the whole input is already on the
+// device (a flag write failed and the rest was copied synchronously), 0
+// when the caller should copy as usual.
 int start_chunked_input(falx_ctx *c, const uint8_t *host_data, uint64_t len) {
     if (c->write_value_state == 0) {
         void *fn = nullptr;
@@ -1278,7 +1280,7 @@ int start_chunked_input(falx_ctx *c, const uint8_t *host_data, uint64_t len) {
                                       c->copy_stream));
             FALX_CUDA(cudaStreamSynchronize(c->copy_stream));
             c->write_value_state = -1;
-            return 0;
+            return 2;
         }
     }
     c->pend_arrive = c->arrive;
@@ -1326,13 +1328,14 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     // Large inputs on the default rows path: copy in chunks on the copy
     // stream and let the index kernel start on the first chunk.
     const bool rows_call = hc || host_out->field_bytes || host_out->stats;
-    bool chunked = false;
+    bool chunked = false, copied = false;
     if (len >= kChunkedInMin && rows_call && c->rows_path == 0 && schema->dialect != FALX_NDJSON) {
         rc = start_chunked_input(c, host_data, len);
         if (rc < 0) return rc;
         chunked = rc == 1;
+        copied = rc == 2;
     }
-    if (len && !chunked) FALX_CUDA(cudaMemcpyAsync(c->dev_in, host_data, len, cudaMemcpyHostToDevice, c->stream));
+    if (len && !chunked && !copied) FALX_CUDA(cudaMemcpyAsync(c->dev_in, host_data, len, cudaMemcpyHostToDevice, c->stream));
     falx_outputs d = *host_out;
     falx_columns dc;
     if (host_out->index_cap) d.index = (uint32_t *)(dout + o_index);
@@ -1900,8 +1903,12 @@ int falx_index_structurals_speculative(falx_ctx *c, const falx_model *md, int di
 // driver's allocation locks. For them this entry point runs the same index
 // kernel as falx_index_structurals without a context: its look-back scratch
 // (one status record per 16 KiB tile plus a small header) lives in the
-// file-scope array below, reserved when the library is loaded. Every GPU
-// that loads the library holds those bytes until the process exits.
+// file-scope array below. Under CUDA's default lazy module loading the
+// driver places that array in device memory on the first call on each
+// device (the cudaGetSymbolAddress in noalloc_setup), so that first call
+// can still fail for lack of memory: callers make one call early, before
+// memory is full or frozen. From then on the device holds those bytes until
+// the process exits, and no call allocates.
 // ===========================================================================
 namespace {
 
@@ -1957,7 +1964,11 @@ int noalloc_setup(int device) {
     if (!rc) rc = noalloc_setup_kernel<D_NDJSON>(dv);
     if (rc) return rc;
     dv.scratch = static_cast<NoAllocScratch *>(ptr);
-    dv.epoch = 0;
+    // FALX_NOALLOC_EPOCH_START (tests only) starts the epoch near its wrap
+    // so the clearing path below runs within a few calls.
+    const char *e0 = getenv("FALX_NOALLOC_EPOCH_START");
+    dv.epoch = e0 ? (uint32_t)strtoul(e0, nullptr, 0) : 0;
+    if (dv.epoch >= (1u << 28)) dv.epoch = 0;
     dv.ready = true;
     return FALX_OK;
 }

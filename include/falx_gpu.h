@@ -390,9 +390,13 @@ int falx_batch_plan(const uint64_t *lens, uint32_t ndocs, uint32_t chunk_bytes, 
  * process exits), so inputs are limited to FALX_NOALLOC_MAX_BYTES
  * (FALX_ERR_INPUT_TOO_LARGE beyond). `data` and `out` are device pointers in
  * `device`; `stream` is a cudaStream_t (NULL = legacy default stream); the
- * call returns after the stream has drained. The first call on a device also
- * sets that device up (looks up the scratch address, sets kernel
- * attributes), so make it before any stream capture. All calls share the
+ * call synchronises `stream` and returns after it has drained. The first
+ * call on a device also sets that device up (looks up the scratch address,
+ * sets kernel attributes), so make it before any stream capture. Under
+ * CUDA's default lazy module loading the driver places the scratch array in
+ * device memory during that first call, which can therefore still fail for
+ * lack of memory: make it early, before memory is full or frozen; later
+ * calls allocate nothing. All calls share the
  * one scratch array: calls whose work can overlap on a GPU (other host
  * threads, other streams) race and must be serialised by the caller.
  * Output is identical to falx_index_structurals. */
