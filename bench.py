@@ -725,6 +725,173 @@ def bench_batch(eng, args):
     }
 
 
+def bench_sharded(args):
+    """One file over N GPUs (torchrun, one rank per GPU): the file is N
+    seeded csv_hash documents of --size bytes, cut mid-document so the seams
+    fall inside records; rank r's shard runs from the middle of document r
+    to the middle of document r + 1 (about --size bytes: per-GPU work is
+    fixed and the file grows with N). A step on every rank: shard summary,
+    summary exchange, first record start, start exchange, one falx_parse
+    over the rank's records (index + tape + field bytes + columns; the last
+    record's bytes past the shard come from host memory), then the exchange
+    of row and arena counts that places the part in the global table. Each
+    exchange is one all-gather (NCCL; gloo when ranks share a GPU)."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import falx_gb300 as fx
+    import oracle
+    from falx_gb300 import gen, shards
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    ndev = torch.cuda.device_count()
+    gpu_id = local % ndev
+    torch.cuda.set_device(gpu_id)
+    shared = world > ndev  # ranks sharing a GPU: exercises the path only, exchanges over gloo
+    dist.init_process_group("gloo" if shared else "nccl")
+    dev = torch.device("cuda", gpu_id)
+    gdev = "cpu" if shared else dev
+
+    def gather(o):
+        return shards.fixed_all_gather(o, gdev)
+
+    docs = {k: gen.generate(gen.CSV_HASH, args.size, seed=0x5EED0 + k) for k in (rank, rank + 1) if k < world}
+    lens = gather(int(docs[rank].size))
+    doc_at = [sum(lens[:k]) for k in range(world + 1)]
+    file_len = doc_at[world]
+    cut = [0] + [doc_at[k] + lens[k] // 2 for k in range(1, world)] + [file_len]
+    lo, hi = cut[rank], cut[rank + 1]
+
+    def read(a, b):
+        parts = []
+        for k, d in docs.items():
+            s0, s1 = max(a, doc_at[k]), min(b, doc_at[k] + d.size)
+            if s0 < s1:
+                parts.append(d[s0 - doc_at[k]: s1 - doc_at[k]].tobytes())
+        data = b"".join(parts)
+        if len(data) != b - a:
+            raise RuntimeError("bytes %d..%d are not held by rank %d" % (a, b, rank))
+        return data
+
+    host_shard = np.frombuffer(read(lo, hi), dtype=np.uint8)
+    prev = read(lo - 1, lo)[0] if lo else -1
+    pinned = torch.empty(host_shard.size, dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = host_shard
+    buf = torch.empty(host_shard.size + (1 << 20), dtype=torch.uint8, device=dev)  # room for the last record
+    shard = buf[: host_shard.size]
+    shard.copy_(pinned)
+    eng = fx.Engine(gpu_id)
+    eng._sync_stream()
+    gpu = shards.GpuShards(eng, full=True)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return shards.parse_columns_sharded(gpu, shard, fx.CSV_HASH, SCHEMA_COLS, rank, lo, prev, file_len, read,
+                                            gather)
+
+    def outputs():
+        last = gpu.last
+        outs = [last["index"], last["seps"], last["ends"]]
+        for k in range(len(SCHEMA_COLS)):
+            outs.extend(last["columns"].column(k).values())
+        return [o.reshape(-1).view(torch.uint8) for o in outs]
+
+    for _ in range(max(args.warmup, 3)):
+        part = step()
+    torch.cuda.synchronize()
+    dist.barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    per = []
+    with Clocks(gpu_id) as clk:
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            ev0.record(stream)
+            part = step()
+            ev1.record(stream)
+            ev1.synchronize()
+            per.append(ev0.elapsed_time(ev1))
+        t_wall = time.perf_counter() - t_wall
+    dist.barrier()
+    t = torch.tensor([sum(per) / len(per)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    value = file_len / GIB / (ms / 1e3)
+
+    # End to end: each step copies the shard in from pinned host memory and
+    # the part's outputs back into pinned host buffers.
+    h_outs = [torch.empty(max(o.numel(), 1), dtype=torch.uint8, pin_memory=True) for o in outputs()]
+    d2h = sum(o.numel() for o in outputs())
+    e2e_t = []
+    for _ in range(max(3, min(args.steps, 7))):
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        shard.copy_(pinned, non_blocking=True)
+        step()
+        for h, o in zip(h_outs, outputs()):
+            if o.numel():
+                h[: o.numel()].copy_(o, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - s0)
+    t = torch.tensor([float(np.median(e2e_t))], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_s = float(t.item())
+
+    # Parity: every rank checks its part against the CPU port over the
+    # part's bytes; rank 0 checks that the parts tile the file.
+    mism = []
+    if not args.no_cpu:
+        a, b = part["bounds"]
+        piece = np.frombuffer(read(a, b), dtype=np.uint8) if b > a else np.zeros(0, np.uint8)
+        ref = run_cpu(piece, max(1, (os.cpu_count() or 1) // max(1, min(world, ndev))))
+        last = gpu.last
+        if not np.array_equal(last["index"].cpu().numpy().view(np.uint32), ref["index"]):
+            mism.append("rank %d: structural index" % rank)
+        if (last["field_bytes"].fields, last["field_bytes"].bytes) != tuple(ref["field_bytes"]):
+            mism.append("rank %d: field bytes" % rank)
+        cols = last["columns"]
+        compare_columns(host_columns(SCHEMA_COLS, cols._bufs, cols.rows, cols._str_lens), ref["columns"],
+                        SCHEMA_COLS, cols.rows, ref["rows"], mism)
+    checks = gather((part["bounds"], part["rows"], part["row_at"], mism, d2h))
+    if rank == 0:
+        bounds = [c[0] for c in checks]
+        tiled = bounds[0][0] == 0 and bounds[-1][1] == file_len and all(
+            p[1] == q[0] for p, q in zip(bounds, bounds[1:]))
+        placed = all(checks[r][2] == sum(c[1] for c in checks[:r]) for r in range(world))
+        allm = [m for c in checks for m in c[3]] + ([] if tiled else ["parts do not tile the file"]) + \
+            ([] if placed else ["row offsets"])
+        parity = {"status": "unchecked", "why": "--no-cpu"} if args.no_cpu else \
+            {"status": "ok" if not allm else "mismatch", "mismatches": allm,
+             "checked": "every rank's index, field bytes and columns against the CPU port over its part's bytes; "
+                        "parts tile the file; row offsets"}
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": "GiB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": WORKLOAD.replace("1 GiB", "%d x %d-byte documents, one file" % (world, args.size)),
+                       "input": "each rank's shard device-resident (value); pinned host memory (e2e)",
+                       "bytes": int(file_len), "bytes_per_rank": [int(c[0][1] - c[0][0]) for c in checks],
+                       "rows": int(sum(c[1] for c in checks)), "l2": "shards of 1 GiB > L2, no flush",
+                       "parallelism": "shards of one file, %d ranks%s" % (world, " on shared GPUs" if shared else "")},
+            "cpu_baseline": None,
+            "parity": parity,
+            "e2e": {"value": round(file_len / GIB / e2e_s, 4), "unit": "GiB/s",
+                    "h2d_bytes_per_step": int(file_len), "d2h_bytes_per_step": int(sum(c[4] for c in checks)),
+                    "ms_per_step": round(e2e_s * 1e3, 3)},
+            # per rank and step: shard summary (2), first-record window (1; none on rank 0), falx_parse (2)
+            "gpu_launches": args.steps * (5 * world - 1),
+            "clocks": clk.summary(),
+            "wall_s": round(t_wall, 3),
+        }
+        print(json.dumps(line))
+    dist.barrier()
+    eng.close()
+    dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -739,6 +906,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         bench_reference(args)
+    elif int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        bench_sharded(args)
     else:
         bench_gpu(args)
 

@@ -203,7 +203,8 @@ class Engine:
 
     def parse_all(self, data, schema, stats_fields=(4, 5)):
         """Every output of one fused falx_parse pass: structural index, tape,
-        columns, field-byte counts and count/sum stats."""
+        columns, field-byte counts and count/sum stats (stats_fields=None
+        leaves the stats out)."""
         torch = self.torch
         d = self.to_device(data)
         n = d.numel()
@@ -225,8 +226,9 @@ class Engine:
             out.ends, out.ends_cap = ends.data_ptr(), ecap
             out.columns = ctypes.pointer(cols)
             out.field_bytes = ctypes.pointer(fb)
-            out.stats = ctypes.pointer(st)
-            out.stats_fields[0], out.stats_fields[1] = stats_fields
+            if stats_fields is not None:
+                out.stats = ctypes.pointer(st)
+                out.stats_fields[0], out.stats_fields[1] = stats_fields
             rc = self.lib.falx_parse(self.ctx, byref(cs), c_void_p(d.data_ptr()), n, byref(out))
             if rc == _lib.FALX_ERR_CAPACITY:
                 icap, scap, ecap = max(icap, out.n_index), max(scap, out.n_seps), max(ecap, out.n_ends)
@@ -236,7 +238,8 @@ class Engine:
             check(rc, "falx_parse")
             columns = Columns(schema, cols.rows, bufs, [cols.cols[k].str_len for k in range(len(schema.columns))], d)
             return {"index": index[: out.n_index], "seps": seps[: out.n_seps], "ends": ends[: out.n_ends],
-                    "columns": columns, "field_bytes": FieldByteStats(fb.fields, fb.bytes), "stats": GeoStats(st)}
+                    "columns": columns, "field_bytes": FieldByteStats(fb.fields, fb.bytes),
+                    "stats": GeoStats(st) if stats_fields is not None else None}
 
     # ---- learned speculation -------------------------------------------
     def model_create(self, seed=1):

@@ -140,3 +140,57 @@ def test_gloo_rank_failure_is_detected(tmp_path):
     assert not alive, "a rank hung"
     assert time.time() - t0 < 60
     assert open(path).read().startswith("detected")
+
+
+COL_CASES = [(gen.CSV_HASH, 1, [(0, 1), (1, 3), (3, 1), (4, 2), (5, 2), (2, 4)]),
+             (gen.CSV_GEO, 0, [(1, 3), (4, 2), (5, 2), (0, 0)]),
+             (gen.ADVERSARIAL, 1, [(0, 3), (1, 4), (2, 2)]),
+             (gen.TSV, 2, [(0, 3), (1, 0), (2, 4)]),
+             (gen.LOGFMT, 3, [(0, 3), (1, 3), (3, 4)])]
+
+
+def assert_table(got, want, columns, ctx):
+    rows, cols = got
+    wrows, wcols = want
+    assert rows == wrows, ctx
+    for k, (f, t) in enumerate(columns):
+        g, w = cols[k], wcols[k]
+        assert np.array_equal(g["valid"][: (rows + 63) // 64], w["valid"][: (rows + 63) // 64]), (ctx, k)
+        if t == 3:
+            assert np.array_equal(g["offsets"], w["offsets"]) and g["data"] == w["data"], (ctx, k)
+        elif t == 4:
+            assert np.array_equal(np.asarray(g["spans"]).reshape(-1, 2), np.asarray(w["spans"]).reshape(-1, 2)), (ctx, k)
+        else:
+            assert np.array_equal(np.asarray(g["values"]).view(np.uint8), np.asarray(w["values"]).view(np.uint8)), \
+                (ctx, k)
+
+
+@pytest.mark.parametrize("kind,dialect,columns", COL_CASES)
+def test_simulated_world_columns(kind, dialect, columns):
+    from shard_oracle import sharded_columns
+
+    doc = bytes(gen.generate(kind, 256 << 10))
+    want = oracle.parse_columns(doc, dialect, columns)
+    rng = np.random.default_rng(kind * 11 + dialect)
+    for world in (1, 2, 3, 5):
+        for _ in range(3):
+            bounds = cut_points(len(doc), rng, world)
+            got = sharded_columns(doc, dialect, columns, bounds, OracleShards())
+            assert_table(got, want, columns, (world, bounds))
+
+
+def test_columns_seams():
+    # seams inside quotes, comments, escapes, right after '\n', 1-byte and
+    # empty shards, shards without a record start, a file without a final newline
+    from shard_oracle import sharded_columns
+
+    doc = b'a,"x\n#y",b\n#c,"d\n"e,f\n"g\\\\"h\n1,"2""3",4\n' * 40 + b'last,"open'
+    for dialect in (0, 1, 3):
+        cols = [(0, 3), (1, 3), (2, 4)]
+        want = oracle.parse_columns(doc, dialect, cols)
+        for step in (1, 2, 3, 7, 13, 101):
+            bounds = [(i, min(i + step, len(doc))) for i in range(0, len(doc), step)][:30]
+            bounds[-1] = (bounds[-1][0], len(doc))
+            bounds.insert(3, (bounds[2][1], bounds[2][1]))
+            got = sharded_columns(doc, dialect, cols, bounds, OracleShards())
+            assert_table(got, want, cols, (dialect, step))
