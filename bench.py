@@ -727,10 +727,10 @@ def bench_batch(eng, args):
 
 def bench_sharded(args):
     """One file over N GPUs (torchrun, one rank per GPU): the file is N
-    seeded csv_hash documents of --size bytes, cut mid-document so the seams
-    fall inside records; rank r's shard runs from the middle of document r
-    to the middle of document r + 1 (about --size bytes: per-GPU work is
-    fixed and the file grows with N). A step on every rank: shard summary,
+    seeded csv_hash documents of --size bytes, cut a little way into each
+    document so the seams fall inside records; rank r's shard runs from that
+    point in document r to the same point in document r + 1 (about --size
+    bytes: per-GPU work is fixed and the file grows with N). A step on every rank: shard summary,
     summary exchange, first record start, start exchange, one falx_parse
     over the rank's records (index + tape + field bytes + columns; the last
     record's bytes past the shard come from host memory), then the exchange
@@ -762,7 +762,8 @@ def bench_sharded(args):
     lens = gather(int(docs[rank].size))
     doc_at = [sum(lens[:k]) for k in range(world + 1)]
     file_len = doc_at[world]
-    cut = [0] + [doc_at[k] + lens[k] // 2 for k in range(1, world)] + [file_len]
+    # seams a little way into documents 1 .. N-1, inside a record
+    cut = [0] + [doc_at[k] + (64 << 10) + 977 * k for k in range(1, world)] + [file_len]
     lo, hi = cut[rank], cut[rank + 1]
 
     def read(a, b):

@@ -134,13 +134,15 @@ class Engine:
         d = self.to_device(data)
         n = d.numel()
         self._sync_stream()
-        scap, ecap = n // 4 + 1024, n // 16 + 1024
         if reuse is not None:
-            scap, ecap = max(scap, reuse[0].numel()), max(ecap, reuse[1].numel())
+            # the recycled buffers first; larger ones only if the tape needs them
+            seps, ends = reuse
+            scap, ecap = seps.numel(), ends.numel()
+        else:
+            scap, ecap = n // 4 + 1024, n // 16 + 1024
+            seps, ends = None, None
         while True:
-            if reuse is not None and reuse[0].numel() >= scap and reuse[1].numel() >= ecap:
-                seps, ends = reuse
-            else:
+            if seps is None:
                 seps = self.empty(scap, self.torch.int32)
                 ends = self.empty(ecap, self.torch.int64)
             ns, ne = c_uint64(), c_uint64()
@@ -148,6 +150,7 @@ class Engine:
                                           scap, c_void_p(ends.data_ptr()), ecap, byref(ns), byref(ne))
             if rc == _lib.FALX_ERR_CAPACITY:
                 scap, ecap = max(scap, ns.value), max(ecap, ne.value)
+                seps = None
                 continue
             check(rc, "falx_parse_tape")
             return seps[: ns.value], ends[: ne.value]

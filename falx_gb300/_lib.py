@@ -16,6 +16,7 @@ FALX_ERR_SCHEMA = -4
 FALX_ERR_TIMEOUT = -5
 FALX_ERR_CUDA = -6
 FALX_ERR_OVERFLOW = -7
+FALX_ERR_FORMAT = -8
 
 CSV, CSV_HASH, TSV, LOGFMT, NDJSON = 0, 1, 2, 3, 4
 I64, U32, F64, STR, BYTES = 0, 1, 2, 3, 4
@@ -48,6 +49,10 @@ class falx_geo_text_stats(Structure):
     _fields_ = [("records", c_uint64), ("city_values", c_uint64), ("city_bytes", c_uint64),
                 ("city_checksum", c_uint64), ("latitude_values", c_uint64), ("longitude_values", c_uint64),
                 ("latitude_checksum", c_uint64), ("longitude_checksum", c_uint64)]
+
+
+class falx_gz_block(Structure):
+    _fields_ = [("in_off", c_uint64), ("out_off", c_uint64), ("in_len", c_uint32), ("out_len", c_uint32)]
 
 
 class falx_field_byte_stats(Structure):
@@ -113,6 +118,9 @@ SIGNATURES = {
     "falx_parse_host": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, POINTER(falx_outputs)]),
     "falx_index_structurals_noalloc": (c_int, [c_int, c_int, c_void_p, c_uint64, c_void_p, c_uint64,
                                                POINTER(c_uint64), c_void_p]),
+    "falx_bgzf_scan": (c_int, [c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64), POINTER(c_uint64)]),
+    "falx_bgzf_inflate": (c_int, [c_void_p, c_void_p, c_uint64, c_void_p, c_uint64, c_void_p, c_uint64, c_void_p,
+                                  POINTER(c_uint64)]),
     "falx_model_param_count": (c_uint64, []),
     "falx_model_create": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
     "falx_model_destroy": (None, [c_void_p]),

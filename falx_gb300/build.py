@@ -14,9 +14,9 @@ GPU_LIB = os.path.join(PKG, "libfalx_gpu.so")
 GEN_LIB = os.path.join(PKG, "libfalx_gen.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-GPU_SOURCES = ["falx_gpu.cu", "batch.cu", "batch_nb2.cu", "batch_nb3.cu"]
+GPU_SOURCES = ["falx_gpu.cu", "batch.cu", "batch_nb2.cu", "batch_nb3.cu", "inflate.cu"]
 GPU_DEPS = ["scan_core.cuh", "rows.cuh", "decimal.cuh", "swar.cuh", "pow5_table.h", "ndjson.cuh", "mlp.cuh", "tile.cuh",
-            "context.h", "batch_kernel.cuh", "columns.cuh", "index_pass.cuh"]
+            "context.h", "batch_kernel.cuh", "columns.cuh", "index_pass.cuh", "inflate_core.h"]
 
 
 def _nvcc():

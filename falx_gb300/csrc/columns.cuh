@@ -331,15 +331,33 @@ __device__ __forceinline__ void warp_text_cell(const Win &W, const Rec &x, uint3
 
 // Cleaned bytes of all fields of the warp's records (csv_hash.rs:1207-1230):
 // every byte but the separators and a trailing '\r', less what cleaning
-// removes from quoted fields; the quoted fields are cleaned by the whole
-// warp. All 32 lanes call it (rows or not).
+// removes from quoted fields. Each thread cleans its own short quoted
+// fields; quoted fields longer than kLongCell are cleaned by the whole warp
+// afterwards, so one long field does not hold up a lane. All 32 lanes call
+// it (rows or not).
+constexpr uint32_t kLongCell = 64;
+
 __device__ __forceinline__ uint32_t warp_field_bytes(const Win &W, const Rec &x, int lane) {
     uint32_t tot = x.row ? (x.end2 - x.start) - (x.nf - 1) : 0u;
-    const uint32_t nf = x.row ? x.nf : 0u;
+    const uint32_t nr = x.row ? x.nf : 0u;
+    bool longq = false;
+    uint32_t from = x.start;
+    for (uint32_t f = 0; f < nr; f++) {
+        const uint32_t to = f + 1 < nr ? W.sep(x.sb + f) : x.end2;
+        const uint32_t n = to - from;
+        if (n >= 2 && W.byte(from) == '"') {
+            if (n <= kLongCell) tot -= n - cleaned_len(W.ptr(from, n), n);
+            else longq = true;
+        }
+        from = to + 1;
+    }
+    if (__ballot_sync(0xffffffffu, longq) == 0) return tot;
+    // the long quoted fields, one warp-wide cleaning each
+    const uint32_t nf = longq ? x.nf : 0u;
     uint32_t mx = nf;
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
-    uint32_t from = x.start;
+    from = x.start;
     for (uint32_t f = 0; f < mx; f++) {
         bool quoted = false;
         const uint8_t *src = nullptr;
@@ -347,7 +365,7 @@ __device__ __forceinline__ uint32_t warp_field_bytes(const Win &W, const Rec &x,
         if (f < nf) {
             const uint32_t to = f + 1 < nf ? W.sep(x.sb + f) : x.end2;
             n = to - from;
-            if (n >= 2) {
+            if (n > kLongCell) {
                 src = W.ptr(from, n);
                 quoted = src[0] == '"' && src[n - 1] == '"';
             }

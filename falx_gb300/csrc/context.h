@@ -77,6 +77,10 @@ struct falx_ctx {
     uint32_t col_epoch = 0;         // their tag
     uint64_t stall_test_ns = 0;     // falx_test_stalled_lookback
     int col_grid[5][2] = {};        // persistent columns grid per dialect, without / with the count-sum sink
+    // bgzf inflate: block table, per-block status and failure count
+    void *gz_scratch = nullptr;
+    uint64_t gz_cap = 0;
+    int gz_grid = 0;
     // per-launch timing of the last rows call (FALX_OPT_TIMING)
     int timing = 0;
     cudaEvent_t ev[5] = {};

@@ -988,6 +988,7 @@ const char *falx_strerror(int code) {
     case FALX_ERR_TIMEOUT: return "device-side wait gave up";
     case FALX_ERR_CUDA: return "CUDA runtime error";
     case FALX_ERR_OVERFLOW: return "string arena exceeds 2 GiB";
+    case FALX_ERR_FORMAT: return "malformed bgzf stream or DEFLATE block";
     default: return "unknown error";
     }
 }
@@ -1041,6 +1042,7 @@ void falx_destroy(falx_ctx *c) {
     if (c->tape_seps) cudaFree(c->tape_seps);
     if (c->tape_ends) cudaFree(c->tape_ends);
     if (c->rec_sums) cudaFree(c->rec_sums);
+    if (c->gz_scratch) cudaFree(c->gz_scratch);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->arrive) cudaFree(c->arrive);
     if (c->in_free) cudaEventDestroy(c->in_free);

@@ -38,6 +38,7 @@ extern "C" {
 #define FALX_ERR_TIMEOUT (-5)          /* a device-side wait gave up; outputs undefined */
 #define FALX_ERR_CUDA (-6)             /* CUDA runtime error */
 #define FALX_ERR_OVERFLOW (-7)         /* string arena beyond i32 offsets (2 GiB) */
+#define FALX_ERR_FORMAT (-8)           /* not a bgzf stream, or a block that does not inflate */
 
 /* Dialects (formats.rs:56-185). */
 typedef enum {
@@ -382,6 +383,39 @@ int falx_batch_tune(falx_ctx *ctx, falx_doc *docs, uint32_t ndocs, falx_batch_co
  * (document, first tile, end tile) for document lengths `lens`. */
 int falx_batch_plan(const uint64_t *lens, uint32_t ndocs, uint32_t chunk_bytes, uint32_t *items, uint32_t cap,
                     uint32_t *n_items);
+
+/* ---------------------------------------------------------------------------
+ * bgzf input (bgzf.rs): a stream of gzip members of at most 64 KiB, each a
+ * raw DEFLATE payload with its uncompressed size (ISIZE) in the trailer.
+ * falx_bgzf_scan walks the member headers on the host (bgzf.rs:61 scan) and
+ * lists every non-empty block with its place in the inflated output;
+ * falx_bgzf_inflate inflates all of them on the GPU at once (one warp per
+ * block; bgzf.rs:201 decompress, :209 decompress_par) into one contiguous
+ * buffer, which the parse entry points then read in place, so the text
+ * never crosses the host link (bgzf.rs:538 parse_gz_par,
+ * examples/gpu_pipeline.rs:1-8). As in the reference, ISIZE must equal the
+ * inflated length and the CRC is not checked.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    uint64_t in_off;   /* raw DEFLATE payload: offset in the compressed stream */
+    uint64_t out_off;  /* offset of the block's bytes in the inflated output */
+    uint32_t in_len;   /* payload bytes */
+    uint32_t out_len;  /* ISIZE */
+} falx_gz_block;
+
+/* Host only. FALX_ERR_FORMAT for a malformed stream; FALX_ERR_CAPACITY (with
+ * *n_blocks and *out_len set) when `cap` is too small. */
+int falx_bgzf_scan(const uint8_t *comp, uint64_t len, falx_gz_block *blocks, uint64_t cap, uint64_t *n_blocks,
+                   uint64_t *out_len);
+/* `comp` and `out` are device pointers, `blocks` host memory (copied to the
+ * device). Returns FALX_ERR_FORMAT when a block fails to inflate;
+ * block_status (host, n_blocks entries, optional) then says which: 0 ok,
+ * 1 truncated, 2 reserved block type, 3 stored length mismatch, 4 bad code
+ * lengths, 5 invalid symbol, 6 distance before the block start, 7 more
+ * output than ISIZE, 8 less output than ISIZE, 9 block outside the buffers.
+ * Synchronous on the context's stream. */
+int falx_bgzf_inflate(falx_ctx *ctx, const uint8_t *comp, uint64_t comp_len, const falx_gz_block *blocks,
+                      uint64_t n_blocks, uint8_t *out, uint64_t out_cap, int32_t *block_status, uint64_t *n_failed);
 
 /* Structural index without any allocation (no counterpart in the
  * reference, whose callers are Rust code that allocates freely). For callers

@@ -91,6 +91,12 @@ def lib():
                                          POINTER(orc_text_stats)]
         l.falx_gen.restype = c_uint64
         l.falx_gen.argtypes = [c_int, c_uint64, c_uint64, c_void_p, c_uint64, c_int]
+        l.orc_inflate.restype = c_int
+        l.orc_inflate.argtypes = [c_void_p, c_uint64, c_void_p, c_uint64]
+        l.orc_bgzf_scan.restype = c_int64
+        l.orc_bgzf_scan.argtypes = [c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64)]
+        l.orc_bgzf_inflate_par.restype = c_uint64
+        l.orc_bgzf_inflate_par.argtypes = [c_void_p, c_void_p, c_uint64, c_void_p, c_void_p, c_int]
         l.orc_par_field_bytes.restype = None
         l.orc_par_field_bytes.argtypes = [c_int, c_void_p, c_uint64, c_int, POINTER(c_uint64), POINTER(c_uint64)]
         _lib = l
@@ -323,3 +329,43 @@ def generate(kind, target_bytes, seed=None, threads=None):
     if n > buf.size:
         raise ValueError("output buffer too small")
     return buf[:n]
+
+
+# ---- raw DEFLATE / bgzf (inflate.c)
+GZ_BLOCK = np.dtype([("in_off", "<u8"), ("out_off", "<u8"), ("in_len", "<u4"), ("out_len", "<u4")])
+
+
+def inflate(payload, out_len):
+    """(status, bytes) of one raw DEFLATE stream of out_len bytes."""
+    a, p, n = _buf(payload)
+    out = np.zeros(max(out_len, 1), dtype=np.uint8)
+    rc = lib().orc_inflate(p, n, out.ctypes.data_as(c_void_p), out_len)
+    return rc, out[:out_len].tobytes()
+
+
+def bgzf_scan(comp):
+    """Structured array of the non-empty members (in_off, out_off, in_len,
+    out_len) and the inflated length, or None if malformed."""
+    a, p, n = _buf(comp)
+    total = c_uint64()
+    k = lib().orc_bgzf_scan(p, n, None, 0, byref(total))
+    if k < 0:
+        return None, 0
+    blocks = np.zeros(max(k, 1), dtype=GZ_BLOCK)
+    lib().orc_bgzf_scan(p, n, blocks.ctypes.data_as(c_void_p), k, byref(total))
+    return blocks[:k], total.value
+
+
+def bgzf_inflate_par(comp, threads=0):
+    """(inflated uint8 array, per-block status) of a bgzf stream."""
+    import os
+
+    a, p, n = _buf(comp)
+    blocks, total = bgzf_scan(a)
+    if blocks is None:
+        raise ValueError("not a bgzf stream")
+    out = np.empty(max(total, 1), dtype=np.uint8)
+    status = np.zeros(max(len(blocks), 1), dtype=np.int32)
+    lib().orc_bgzf_inflate_par(p, blocks.ctypes.data_as(c_void_p), len(blocks), out.ctypes.data_as(c_void_p),
+                               status.ctypes.data_as(c_void_p), threads or os.cpu_count() or 1)
+    return out[:total], status[: len(blocks)]

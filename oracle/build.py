@@ -1,5 +1,5 @@
 """Build recipe for the CPU oracle (test infrastructure only): compiles
-oracle.c and oracle_par.c into oracle/_build/liboracle.so. The reference is a
+oracle.c, oracle_par.c and inflate.c into oracle/_build/liboracle.so. The reference is a
 Rust crate and there is no Rust toolchain here or on the GPU hosts, so no
 oracle/_ref build exists."""
 
@@ -13,7 +13,7 @@ LIB = os.path.join(OUT_DIR, "liboracle.so")
 # The synthetic-input generator is compiled in as well (the same C source the
 # package uses), so the CPU reference arm loads no product library.
 GEN_SRC = os.path.join(os.path.dirname(HERE), "falx_gb300", "csrc", "gen.c")
-SOURCES = [os.path.join(HERE, s) for s in ("oracle.c", "oracle_par.c")] + [GEN_SRC]
+SOURCES = [os.path.join(HERE, s) for s in ("oracle.c", "oracle_par.c", "inflate.c")] + [GEN_SRC]
 DEPS = SOURCES + [os.path.join(HERE, "oracle.h"), os.path.abspath(__file__)]
 
 

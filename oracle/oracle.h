@@ -136,6 +136,27 @@ int orc_par_parse(int dialect, const uint8_t *d, uint64_t n, int threads, uint32
 void orc_par_geo_stats(int dialect, const uint8_t *d, uint64_t n, int threads, uint32_t f0, uint32_t f1,
                        orc_geo_stats *out);
 
+/* Raw DEFLATE and bgzf (inflate.c). Status codes, shared with the GPU
+ * decoder's per-block status: */
+#define ORC_Z_TRUNCATED 1
+#define ORC_Z_BLOCK_TYPE 2
+#define ORC_Z_STORED_LEN 3
+#define ORC_Z_CODES 4
+#define ORC_Z_SYMBOL 5
+#define ORC_Z_DISTANCE 6
+#define ORC_Z_OVERFLOW 7
+#define ORC_Z_SIZE 8
+typedef struct {
+    uint64_t in_off, out_off;
+    uint32_t in_len, out_len;
+} orc_gz_block;
+/* 0, or a status above: in[0, n) inflated to exactly out_len bytes */
+int orc_inflate(const uint8_t *in, uint64_t n, uint8_t *out, uint64_t out_len);
+/* the non-empty members; -1 if malformed; *total = inflated bytes */
+int64_t orc_bgzf_scan(const uint8_t *c, uint64_t n, orc_gz_block *out, uint64_t cap, uint64_t *total);
+uint64_t orc_bgzf_inflate_par(const uint8_t *comp, const orc_gz_block *blocks, uint64_t nb, uint8_t *out,
+                              int32_t *status, int threads);
+
 #ifdef __cplusplus
 }
 #endif

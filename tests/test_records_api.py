@@ -57,7 +57,7 @@ def test_fields_match_oracle_tape(engine, dialect):
 
 
 def test_parse_into_recycles(engine):
-    docs = [b"a,b\nc,d\n", b'x,"y\nz",w\n1,2\n3\n', b"", b"only"]
+    docs = [b"a,b\nc,d\n" * 40, b'x,"y\nz",w\n1,2\n3\n', b"", b"only"]
     prev = None
     bufs = None
     for d in docs:
@@ -65,6 +65,8 @@ def test_parse_into_recycles(engine):
         want = [r.fields() for r in fx.parse(d, fx.CSV).records()]
         assert [r.fields() for r in p.records()] == want
         if bufs is not None:
-            assert p._device[0].data_ptr() == bufs[0].data_ptr()  # the recycled device buffers
+            # the recycled device buffers hold the smaller tapes
+            assert p._device[0].data_ptr() == bufs[0].data_ptr()
+            assert p._device[1].data_ptr() == bufs[1].data_ptr()
         bufs = p._device
         prev = p
