@@ -297,6 +297,7 @@ def bench_gpu(args):
     if dist:
         dist.barrier()
     ms = sum(per) / len(per)
+    spread = [round(min(per), 4), round(sorted(per)[len(per) // 2], 4), round(max(per), 4)]
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -381,6 +382,7 @@ def bench_gpu(args):
 
     geo = None if args.no_configs else bench_geo(eng, args, rank)
     nd = None if args.no_configs else bench_ndjson(eng, args, rank)
+    gz = None if args.no_configs else bench_gz(eng, args, rank)
     spec = None if args.no_spec else bench_speculation(eng, args)
     batched = None if args.no_batch else bench_batch(eng, args)
 
@@ -410,7 +412,8 @@ def bench_gpu(args):
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": WORKLOAD, "input": "device-resident (value); pinned host buffers (e2e)",
                    "bytes": n, "structurals": int(n_struct), "rows": int(rows), "tile_bytes": 16384,
-                   "l2": "input 1 GiB > L2, no flush", "parallelism": "replicas" if world > 1 else "single"},
+                   "l2": "input 1 GiB > L2, no flush", "parallelism": "replicas" if world > 1 else "single",
+                   "step_ms_min_median_max": spread},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes": int(algo),
@@ -425,6 +428,7 @@ def bench_gpu(args):
         "field_bytes": {"fields": fb.fields, "bytes": fb.bytes},
         "csv_geo": geo,
         "ndjson": nd,
+        "bgzf": gz,
         "learned_speculation": spec,
         "batched": batched,
         "wall_s": round(wall, 3),
@@ -596,6 +600,150 @@ def bench_ndjson(eng, args, rank):
                                 "1e-12 relative"}
     res["cpu_baseline"] = {"value": round(n / GIB / best, 4), "unit": "GiB/s", "cores": threads, "kind": "port",
                            "sample": "the same 1 GiB input, JSON-aware sink, lines split across the threads"}
+    return res
+
+
+def bench_gz(eng, args, rank):
+    """bgzf input (bgzf.rs:538 parse_gz_par; examples/gpu_pipeline.rs): the
+    1 GiB csv_hash document as a bgzf stream (zlib level 6, 65280-byte
+    members). Device-resident compressed bytes: one step = the inflate
+    kernel (every member at once) then falx_parse over the text in place
+    (index + field bytes + columns). The inflate kernel is also timed alone.
+    End to end: the compressed bytes from pinned host memory, the step, the
+    columns and index back. The CPU port inflates the members on all host
+    threads and parses the text; its output is compared with the GPU's."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import falx_gb300 as fx
+    from falx_gb300 import _lib, bgzf
+
+    host = make_input(args.size)
+    n = int(host.size)
+    t0 = time.perf_counter()
+    comp = bgzf.compress(host.tobytes(), 6, threads=os.cpu_count() or 8)
+    comp_s = time.perf_counter() - t0
+    blocks, total = bgzf.scan(comp)
+    assert total == n
+    pinned = torch.empty(len(comp), dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = np.frombuffer(comp, dtype=np.uint8)
+    dcomp = pinned.to("cuda")
+    text = torch.empty(n, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    eng._sync_stream()
+    schema = fx.Schema(fx.CSV_HASH, SCHEMA_COLS)
+    bptr = blocks.ctypes.data_as(ctypes.c_void_p)
+    failed = ctypes.c_uint64()
+
+    def inflate():
+        _lib.check(eng.lib.falx_bgzf_inflate(eng.ctx, ctypes.c_void_p(dcomp.data_ptr()), dcomp.numel(), bptr,
+                                             len(blocks), ctypes.c_void_p(text.data_ptr()), n, None,
+                                             ctypes.byref(failed)), "falx_bgzf_inflate")
+
+    res_box = {}
+
+    def step():
+        inflate()
+        res_box["r"] = eng.parse_all(text, schema, stats_fields=None)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per, per_inf = [], []
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            ev0.record(stream)
+            inflate()
+            ev1.record(stream)
+            ev1.synchronize()
+            per_inf.append(ev0.elapsed_time(ev1))
+        for _ in range(args.steps):
+            ev0.record(stream)
+            step()
+            ev1.record(stream)
+            ev1.synchronize()
+            per.append(ev0.elapsed_time(ev1))
+    ms, ms_inf = sum(per) / len(per), sum(per_inf) / len(per_inf)
+    r = res_box["r"]
+    # end to end: compressed bytes in from pinned memory, index and columns out
+    outs = [r["index"]] + [v for k in range(len(SCHEMA_COLS)) for v in r["columns"].column(k).values()]
+    h_outs = [torch.empty(max(o.numel() * o.element_size(), 1), dtype=torch.uint8, pin_memory=True) for o in outs]
+    d2h = sum(o.numel() * o.element_size() for o in outs)
+    e2e_t = []
+    for _ in range(max(3, min(args.steps, 7))):
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        dcomp.copy_(pinned, non_blocking=True)
+        step()
+        rr = res_box["r"]
+        cur = [rr["index"]] + [v for k in range(len(SCHEMA_COLS)) for v in rr["columns"].column(k).values()]
+        for h, o in zip(h_outs, cur):
+            if o.numel():
+                h[: o.numel() * o.element_size()].copy_(o.reshape(-1).view(torch.uint8), non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - s0)
+    e2e_s = float(np.median(e2e_t))
+    peak, peak_kind = peaks()
+    algo_inf = len(comp) + n
+    res = {"workload": "csv_hash 1 GiB as bgzf (zlib level 6, %d members of up to 65280 bytes, %d compressed "
+                       "bytes): inflate on the GPU, then index + field bytes + typed columns over the text in "
+                       "place" % (len(blocks), len(comp)),
+           "value": round(n / GIB / (ms / 1e3), 3), "unit": "GiB/s (uncompressed)", "ms": round(ms, 4),
+           "inflate": {"value": round(n / GIB / (ms_inf / 1e3), 3), "unit": "GiB/s (uncompressed)",
+                       "ms": round(ms_inf, 4),
+                       "roofline": {"bound": "issue (serial Huffman decode per member)",
+                                    "achieved": round(algo_inf / (ms_inf / 1e3) / 1e9, 1), "peak": peak,
+                                    "unit": "GB/s", "frac": round(algo_inf / (ms_inf / 1e3) / 1e9 / peak, 4),
+                                    "algorithmic_bytes": algo_inf, "peak_kind": peak_kind,
+                                    "note": "compressed bytes read + text written, against the HBM copy peak"}},
+           "ratio": round(n / len(comp), 3), "bytes": n, "compressed_bytes": len(comp),
+           "e2e": {"value": round(n / GIB / e2e_s, 3), "unit": "GiB/s (uncompressed)",
+                   "h2d_bytes_per_step": len(comp), "d2h_bytes_per_step": int(d2h),
+                   "ms_per_step": round(e2e_s * 1e3, 3)},
+           "compress_s_host": round(comp_s, 2), "l2": "text 1 GiB > L2, no flush", "clocks": clk.summary()}
+    if rank != 0 or args.no_cpu:
+        return res
+    import oracle
+
+    threads = os.cpu_count() or 1
+
+    def cpu():
+        out, st = oracle.bgzf_inflate_par(comp, threads)
+        return oracle.parse_par(out, oracle.CSV_HASH, SCHEMA_COLS, threads), int(st.sum())
+
+    best, (ref, bad) = timed_best(cpu)
+    t_inf, _ = timed_best(lambda: oracle.bgzf_inflate_par(comp, threads))
+
+    def zlib_par():
+        import zlib
+        from concurrent.futures import ThreadPoolExecutor
+
+        mv = memoryview(comp)
+        with ThreadPoolExecutor(threads) as ex:
+            return list(ex.map(lambda b: zlib.decompress(mv[int(b["in_off"]): int(b["in_off"]) + int(b["in_len"])],
+                                                         -15), blocks))
+
+    t_zlib, _ = timed_best(zlib_par)
+    mism = []
+    if bad:
+        mism.append("CPU port failed %d members" % bad)
+    if not np.array_equal(r["index"].cpu().numpy().view(np.uint32), ref["index"]):
+        mism.append("structural index")
+    if (r["field_bytes"].fields, r["field_bytes"].bytes) != tuple(ref["field_bytes"]):
+        mism.append("field bytes")
+    cols = r["columns"]
+    compare_columns(host_columns(SCHEMA_COLS, cols._bufs, cols.rows, cols._str_lens), ref["columns"], SCHEMA_COLS,
+                    cols.rows, ref["rows"], mism)
+    res["parity"] = {"status": "ok" if not mism else "mismatch", "mismatches": mism,
+                     "checked": "index, field bytes and every column of the text inflated on the GPU against "
+                                "the CPU port's inflate + parse of the same stream"}
+    res["cpu_baseline"] = {"value": round(n / GIB / best, 4), "unit": "GiB/s (uncompressed)", "cores": threads,
+                           "kind": "port", "isa": cpu_isa(),
+                           "sample": "the same bgzf stream: members inflated on all threads, then the parse",
+                           "inflate_only": round(n / GIB / t_inf, 4),
+                           "zlib_inflate_only": round(n / GIB / t_zlib, 4)}
     return res
 
 

@@ -20,30 +20,20 @@ namespace {
 constexpr int kGzWarps = 8;
 constexpr int kGzThreads = 32 * kGzWarps;
 
-// The warp's view of the decoder's output: pending literals one per lane,
-// flushed with one store; matches and stored runs copied by all lanes.
+// The warp's view of the decoder's output: a literal is stored by lane 0;
+// a match (after a barrier that makes lane 0's stores visible to the warp)
+// and a stored run are copied by all lanes.
 struct WarpSink {
     uint8_t *out;
     uint32_t lane;
-    uint32_t lit;      // this lane's pending literal
-    uint32_t nlit;     // pending literals (warp-uniform)
-    uint32_t lit_pos;  // position of the first pending literal
 
     __device__ __forceinline__ void sync() { __syncwarp(); }
-    __device__ __forceinline__ void flush() {
-        if (nlit) {
-            if (lane < nlit) out[lit_pos + lane] = (uint8_t)lit;
-            nlit = 0;
-            __syncwarp();
-        }
-    }
+    __device__ __forceinline__ void flush() { __syncwarp(); }
     __device__ __forceinline__ void literal(uint32_t pos, uint32_t c) {
-        if (nlit == 0) lit_pos = pos;
-        if (lane == nlit) lit = c;
-        if (++nlit == 32) flush();
+        if (lane == 0) out[pos] = (uint8_t)c;
     }
     __device__ __forceinline__ void match(uint32_t pos, uint32_t dist, uint32_t len) {
-        flush();
+        __syncwarp();
         const uint8_t *src = out + (pos - dist);
         if (dist >= len) {
             for (uint32_t k = lane; k < len; k += 32) out[pos + k] = src[k];
@@ -53,7 +43,7 @@ struct WarpSink {
         __syncwarp();
     }
     __device__ __forceinline__ void stored(const uint8_t *s, uint32_t pos, uint32_t len) {
-        flush();
+        __syncwarp();
         for (uint32_t k = lane; k < len; k += 32) out[pos + k] = s[k];
         __syncwarp();
     }
@@ -81,7 +71,7 @@ __global__ void __launch_bounds__(kGzThreads) inflate_kernel(const uint8_t *comp
             rc = ERR_BOUNDS;
         } else {
             Bits bits{comp + B.in_off, B.in_len, 0u, 0ull, 0, false};
-            WarpSink sink{out + B.out_off, lane, 0u, 0u, 0u};
+            WarpSink sink{out + B.out_off, lane};
             rc = inflate_stream(bits, T[warp], K, sink, B.out_len);
         }
         if (lane == 0) {

@@ -8,8 +8,8 @@
 // The decoder is warp-uniform: every lane runs the same bit reader, table
 // lookups and bounds checks on the same values, so the warp never diverges
 // while it decodes; the work that is parallel goes to the lanes through the
-// Sink: literal runs are collected one byte per lane and written with one
-// store, a match's bytes are copied by all lanes at once (byte k of a match
+// Sink: a literal is stored by one lane, a match's bytes are copied by all
+// lanes at once (byte k of a match
 // at distance d comes from position pos - d + k mod d, which is already
 // written, so the copy has no dependencies inside it), and the fast decode
 // tables are filled one entry per lane.
@@ -82,16 +82,25 @@ struct Bits {
     int32_t cnt;   // bits in buf that came from the payload
     bool bad;      // a read went past the payload
 
+    // Keeps at least 33 bits buffered while input remains. Away from the
+    // payload's ends, 4 bytes at any alignment come from the two aligned
+    // words that hold them (both inside the payload: pos >= 4 and
+    // pos + 8 <= n); near the ends, one byte at a time.
     GZ_HD void refill() {
+        if (cnt > 32) return;
+        if (pos >= 4 && pos + 8 <= n) {
+            const uintptr_t a = (uintptr_t)(p + pos);
+            const uint32_t *w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+            const uint32_t sh = 8u * (uint32_t)(a & 3u);
+            const uint32_t v = sh ? (w[0] >> sh) | (w[1] << (32u - sh)) : w[0];
+            buf |= (uint64_t)v << cnt;
+            pos += 4;
+            cnt += 32;
+            return;
+        }
         while (cnt <= 56 && pos < n) {
-            if (cnt <= 32 && pos + 4 <= n && ((uintptr_t)(p + pos) & 3u) == 0) {
-                buf |= (uint64_t)(*reinterpret_cast<const uint32_t *>(p + pos)) << cnt;
-                pos += 4;
-                cnt += 32;
-            } else {
-                buf |= (uint64_t)p[pos++] << cnt;
-                cnt += 8;
-            }
+            buf |= (uint64_t)p[pos++] << cnt;
+            cnt += 8;
         }
     }
     GZ_HD uint32_t peek(int k) const { return (uint32_t)(buf & ((1ull << k) - 1ull)); }
@@ -156,7 +165,8 @@ GZ_HD uint16_t fast_entry(uint32_t i, int F, const uint16_t *count, const uint16
 }
 
 // One symbol: a table lookup, or the canonical walk bit by bit for codes
-// longer than the table. -1 when the bits are no code.
+// longer than the table. 511 (no symbol of either alphabet) when the bits
+// are no code.
 GZ_HD int decode(Bits &b, const uint16_t *fast, int F, const uint16_t *count, const uint16_t *sym) {
     b.refill();
     if (fast) {
@@ -179,7 +189,7 @@ GZ_HD int decode(Bits &b, const uint16_t *fast, int F, const uint16_t *count, co
         code <<= 1;
     }
     b.drop(15);
-    return -1;
+    return 511;
 }
 
 // Code lengths of a dynamic block (RFC 1951 section 3.2.7) into T.lens and
@@ -205,7 +215,7 @@ GZ_HD int read_dynamic(Bits &b, Tables &T, Sink &out, uint32_t &nlen) {
     while (idx < total) {
         const int s = decode(b, nullptr, 0, T.dcount, T.dsym);
         if (b.bad) return ERR_TRUNCATED;
-        if (s < 0) return ERR_SYMBOL;
+        if (s > 18) return ERR_SYMBOL;
         if (s < 16) {
             T.lens[idx++] = (uint8_t)s;
             continue;
@@ -280,30 +290,30 @@ GZ_HD int inflate_stream(Bits &b, Tables &T, const Consts &K, Sink &out, uint32_
                 const int rc = read_dynamic(b, T, out, nlen);
                 if (rc) return rc;
             }
+            // Symbols: a read past the payload sets b.bad and yields zero
+            // bits from then on; every iteration writes output (bounded by
+            // out_len) or leaves the loop, and b.bad is checked when it does.
             for (;;) {
                 int s = decode(b, T.lfast, kLitFast, T.lcount, T.lsym);
-                if (b.bad) return ERR_TRUNCATED;
-                if (s < 0) return ERR_SYMBOL;
                 if (s < 256) {
-                    if (pos >= out_len) return ERR_OVERFLOW;
+                    if (pos >= out_len) return b.bad ? ERR_TRUNCATED : ERR_OVERFLOW;
                     out.literal(pos, (uint32_t)s);
                     pos++;
                     continue;
                 }
                 if (s == 256) break;
                 s -= 257;
-                if (s >= 29) return ERR_SYMBOL;
+                if (s >= 29) return b.bad ? ERR_TRUNCATED : ERR_SYMBOL;
                 const uint32_t len = K.len_base[s] + b.get(K.len_extra[s]);
                 const int ds = decode(b, T.dfast, kDistFast, T.dcount, T.dsym);
-                if (b.bad) return ERR_TRUNCATED;
-                if (ds < 0 || ds >= 30) return ERR_SYMBOL;
+                if (ds >= 30) return b.bad ? ERR_TRUNCATED : ERR_SYMBOL;
                 const uint32_t dist = K.dist_base[ds] + b.get(K.dist_extra[ds]);
-                if (b.bad) return ERR_TRUNCATED;
-                if (dist > pos) return ERR_DISTANCE;
-                if (out_len - pos < len) return ERR_OVERFLOW;
+                if (dist > pos) return b.bad ? ERR_TRUNCATED : ERR_DISTANCE;
+                if (out_len - pos < len) return b.bad ? ERR_TRUNCATED : ERR_OVERFLOW;
                 out.match(pos, dist, len);
                 pos += len;
             }
+            if (b.bad) return ERR_TRUNCATED;
         } else {
             return ERR_BLOCK_TYPE;
         }
