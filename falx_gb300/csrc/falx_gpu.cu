@@ -644,7 +644,9 @@ int launch_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64
                                                          : c->blocks_per_sm[dialect][rows ? 1 : 0];
     if (c->ctas_per_sm > 0 && c->ctas_per_sm < nb) nb = c->ctas_per_sm;
     uint64_t grid = (uint64_t)c->sm_count * (uint64_t)nb;
-    if (grid > tiles) grid = tiles;
+    // the index pass takes its tiles in groups of kIxGroup
+    const uint64_t units = pass ? (tiles + kIxGroup - 1) / kIxGroup : tiles;
+    if (grid > units) grid = units;
     if (grid == 0) grid = 1;
 #define FALX_LAUNCH(D)                                                                            \
     do {                                                                                          \

@@ -1,30 +1,35 @@
 // Structural index and tape in one persistent pass (index_pass_kernel).
 //
-// Each CTA takes the 16 KiB tiles c, c + G, c + 2G, ... of the input (G =
-// resident CTAs, cooperative launch) and splits the work between two kinds
-// of warps that never meet at a CTA-wide barrier:
+// The input is cut into 16 KiB tiles and the tiles into groups of
+// kIxGroup consecutive tiles; a group is the unit of the look-back. Each CTA
+// takes the groups c, c + G, c + 2G, ... (G = resident CTAs, cooperative
+// launch) and splits the work between two kinds of warps that never meet at
+// a CTA-wide barrier:
 //
-//  8 compute warps   local pass of tile i: classify its bytes (64 per
-//                    thread), scan the dialect's region automaton as
+//  8 compute warps   local pass of each tile of group i: classify its bytes
+//                    (64 per thread), scan the dialect's region automaton as
 //                    transfer functions (thread -> warp) and count
 //                    structurals and terminators for every warp entry state;
-//                    the masks go to a ring of kIxSlots tiles in shared
-//                    memory. The last warp to finish composes the tile's
-//                    aggregate (transfer function, counts per entry state),
-//                    publishes it (level 1) and refills the tile buffer.
-//                    Then the output of tile i - kIxSlots + 1: masks under
-//                    its true entry state, index and tape entries.
-//  1 scheduler warp  the look-backs, tile after tile: entry state and
-//                    output offsets of each tile, published at level 2.
-//                    (More scheduler warps measured slower: their polling
-//                    competes for the same status lines in L2.)
+//                    the masks go to a ring of two groups of tiles in shared
+//                    memory. The last warp to finish a tile composes its
+//                    aggregate (transfer function, counts per entry state)
+//                    and refills the tile buffer; after the group's last
+//                    tile it publishes the group's aggregate (level 1). Then
+//                    the output of group i - 1: masks under their true entry
+//                    states, index and tape entries.
+//  1 scheduler warp  the look-backs, group after group: entry state and
+//                    output offsets of each tile, the group's inclusive
+//                    prefix published at level 2. (More scheduler warps
+//                    measured slower: their polling competes for the same
+//                    status lines in L2.)
 //
-// A tile's prefix needs every earlier tile's local pass, so CTAs that ran
-// in step with a one-tile delay would wait for the slowest CTA of each
-// round; with kIxSlots tiles between a local pass and its output, a CTA can
-// run that many tiles ahead of the look-backs and the rounds' jitter
-// averages out. The warps hand over through mbarriers in shared memory
-// (tile bytes landed; aggregate published; look-back done).
+// A look-back costs a few dependent round trips to L2 whatever the size of
+// the unit it places; with single 16 KiB tiles the scheduler warp took
+// longer per tile than the compute warps and set the pace. A group of two
+// tiles halves the look-backs per byte, and with one whole group between a
+// local pass and its output a CTA runs ahead of its look-backs, so the
+// rounds' jitter averages out. The warps hand over through mbarriers in
+// shared memory (tile bytes landed; aggregate published; look-back done).
 // Transfer functions are kept in byte form (byte s = exit state for entry
 // state s), so composing two is one byte permute; warp sums of counts are
 // one redux each. Every wait is bounded.
@@ -46,7 +51,8 @@ namespace falx {
 constexpr int kIxScheds = 1;                           // scheduler warps
 constexpr int kIxThreads = kThreads + 32 * kIxScheds;  // 8 compute warps + the scheduler warp
 constexpr int kIxSched = kWarps;                       // warp index of the scheduler
-constexpr int kIxSlots = 3;                // tiles between a local pass and its output
+constexpr int kIxGroup = 2;                // tiles per look-back
+constexpr int kIxSlots = 2 * kIxGroup;     // ring of tile slots: two groups (slot 2 g + k: tile k of group slot g)
 constexpr int kIxStage = 256;              // staged structurals per warp and batch
 constexpr int kLbPer = 8;                  // look-back: predecessors watched per lane
 constexpr int kLbWin = 32 * kLbPer;        // look-back: predecessors per round of loads
@@ -207,7 +213,7 @@ __device__ __forceinline__ uint32_t ix_function_counts(const Masks &m, uint64_t 
 }
 
 // ---------------------------------------------------------------------------
-// Look-back record of one tile (64 bytes, in the context's tile-status
+// Look-back record of one group (64 bytes, in the context's tile-status
 // array). Each field is written once per launch before the release of its
 // level; the flag carries the launch epoch, so the array is never cleared
 // between launches.
@@ -215,10 +221,10 @@ __device__ __forceinline__ uint32_t ix_function_counts(const Masks &m, uint64_t 
 struct IxStatus {
     uint32_t flag;    // epoch * 4 + level
     uint32_t exit;    // level 2: exit state
-    uint32_t incl_s;  // level 2: structurals up to the tile's end
-    uint32_t incl_t;  // level 2: terminators up to the tile's end
+    uint32_t incl_s;  // level 2: structurals up to the group's end
+    uint32_t incl_t;  // level 2: terminators up to the group's end
     uint32_t func;    // level 1: transfer function (byte form)
-    uint32_t agg[4];  // level 1: per entry state, structurals | terminators << 16
+    uint32_t agg[4];  // level 1: per entry state, structurals | terminators << 16 (below 2^16 each)
     uint32_t pad[7];
 };
 static_assert(sizeof(IxStatus) == sizeof(TileStatus), "tile status records share one array");
@@ -231,13 +237,14 @@ struct IxSmem {
     uint64_t ms[kIxSlots][kThreads], mnl[kIxSlots][kThreads], mq[kIxSlots][kThreads], mx[kIxSlots][kThreads];
     uint32_t mex[kIxSlots][kThreads];
     uint16_t stage[kWarps][kIxStage];       // per warp: a batch of its structurals in rank order
-    uint64_t full[2];                       // per buffer: the tile's bytes have landed (bulk copy)
-    uint64_t pub[kIxSlots];                 // per slot: the tile's aggregate is published
-    uint64_t lb[kIxSlots];                  // per slot: the tile's look-back is done
+    uint64_t full[2];                       // per buffer (tile k of a group): its bytes have landed (bulk copy)
+    uint64_t pub[2];                        // per group slot: the group's aggregate is published
+    uint64_t lb[2];                         // per group slot: the group's look-back is done
     uint32_t wf[kIxSlots][kWarps];          // warp-inclusive transfer functions
     uint32_t wc[kIxSlots][kWarps][4];       // warp counts per warp entry state
     uint32_t wx[kIxSlots][kWarps];          // function of the warps before, within the tile
     uint32_t tf[kIxSlots];                  // the tile's transfer function
+    uint32_t tc[kIxSlots][4];               // the tile's counts per entry state
     uint32_t cnt[kIxSlots];                 // compute warps done with the tile's local pass
     uint32_t base_s[kIxSlots], base_t[kIxSlots];  // structurals / terminators before the tile
     uint32_t went[kIxSlots][kWarps];        // entry state of each warp
@@ -337,10 +344,9 @@ __device__ __forceinline__ void ix_local(const Params &p, IxSmem &S, uint32_t ti
 }
 
 // The last compute warp of a local pass: the tile's transfer function and
-// counts per entry state from the eight warps', published at level 1.
+// counts per entry state from the eight warps', into shared memory.
 template <int D>
-__device__ __forceinline__ void ix_publish(const Params &p, IxSmem &S, IxStatus *st, uint32_t tile, int rs,
-                                           int lane) {
+__device__ __forceinline__ void ix_tile_agg(IxSmem &S, int rs, int lane) {
     constexpr int NS = NStates<D>::value;
     const int w = lane & (kWarps - 1);
     const uint32_t wf = lane < kWarps ? S.wf[rs][w] : kIdB;
@@ -363,16 +369,33 @@ __device__ __forceinline__ void ix_publish(const Params &p, IxSmem &S, IxStatus 
     if (lane < kWarps) S.wx[rs][w] = wx;
     if (lane == 0) {
         S.tf[rs] = tf;
-        IxStatus *me = st + tile;
-        me->func = tf;
 #pragma unroll
-        for (int e = 0; e < NS; e++) me->agg[e] = tot[e];
-        st_release(&me->flag, p.epoch * 4 + 1);
+        for (int e = 0; e < NS; e++) S.tc[rs][e] = tot[e];
     }
 }
 
-// Scheduler warp: entry state of `tile` and the structurals / terminators
-// before it, by a look-back. Returns false if a wait gave up (the error is
+// The group's aggregate from its tiles' (slots rs0 .. rs0 + nt - 1),
+// published at level 1 (one thread).
+template <int D>
+__device__ __forceinline__ void ix_group_publish(const Params &p, IxSmem &S, IxStatus *st, uint32_t group, int rs0,
+                                                 int nt) {
+    constexpr int NS = NStates<D>::value;
+    IxStatus *me = st + group;
+    uint32_t f = kIdB;
+    uint32_t agg[4] = {0, 0, 0, 0};
+    for (int k = 0; k < nt; k++) {
+#pragma unroll
+        for (int e = 0; e < NS; e++) agg[e] += S.tc[rs0 + k][fb_apply(f, (uint32_t)e)];
+        f = fb_compose(f, S.tf[rs0 + k]);
+    }
+    me->func = f;
+#pragma unroll
+    for (int e = 0; e < NS; e++) me->agg[e] = agg[e];
+    st_release(&me->flag, p.epoch * 4 + 1);
+}
+
+// Scheduler warp: entry state of group `tile` and the structurals /
+// terminators before it, by a look-back over the group records. Returns false if a wait gave up (the error is
 // recorded in the header).
 //
 // Two phases. (1) Flags only, newest first, kLbWin per round of relaxed
@@ -482,12 +505,12 @@ __device__ __forceinline__ bool ix_lookback(const Params &p, IxStatus *st, uint3
     return true;
 }
 
-// Scheduler warp, once the tile's aggregate is in: per-warp entry states and
-// offsets of the tile into shared memory, its inclusive prefix published at
-// level 2.
+// Scheduler warp, once the group's aggregate is in: per-warp entry states and
+// offsets of one of its tiles into shared memory. Returns the tile's counts
+// (structurals | terminators << 16) under its entry state.
 template <int D>
-__device__ __forceinline__ void ix_place(const Params &p, IxSmem &S, IxStatus *st, uint32_t tile, int slot, int lane,
-                                         uint32_t entry, uint32_t bs, uint32_t bt) {
+__device__ __forceinline__ uint32_t ix_place(IxSmem &S, int slot, int lane, uint32_t entry, uint32_t bs,
+                                             uint32_t bt) {
     const int w = lane & (kWarps - 1);
     const uint32_t wx = lane < kWarps ? S.wx[slot][w] : kIdB;
     const uint32_t we = fb_apply(wx, entry);
@@ -506,16 +529,8 @@ __device__ __forceinline__ void ix_place(const Params &p, IxSmem &S, IxStatus *s
     if (lane == 0) {
         S.base_s[slot] = bs;
         S.base_t[slot] = bt;
-        IxStatus *me = st + tile;
-        me->exit = fb_apply(S.tf[slot], entry);
-        me->incl_s = bs + (tot & 0xFFFFu);
-        me->incl_t = bt + (tot >> 16);
-        st_release(&me->flag, p.epoch * 4 + 2);
-        if (tile == p.num_tiles - 1) {
-            p.hdr->n_struct = bs + (tot & 0xFFFFu);
-            p.hdr->n_terms = bt + (tot >> 16);
-        }
     }
+    return tot;
 }
 
 // Output of a tile (compute threads, after its look-back): the thread's
@@ -614,87 +629,131 @@ __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_
     IxStatus *const st = reinterpret_cast<IxStatus *>(p.status);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t G = gridDim.x;
-    const uint32_t own = (p.num_tiles - blockIdx.x + G - 1) / G;  // tiles of this CTA (grid <= tiles)
+    const uint32_t groups = (p.num_tiles + kIxGroup - 1) / kIxGroup;
+    const uint32_t own = (groups - blockIdx.x + G - 1) / G;  // groups of this CTA (grid <= groups)
+    // tiles of group g that exist (the last group may be short)
+    auto tiles_of = [&](uint32_t g) -> int {
+        const uint32_t t0 = g * kIxGroup;
+        return (int)min((uint32_t)kIxGroup, p.num_tiles - t0);
+    };
     if (tid == 0) {
         mbar_init(&S.full[0], 1);
         mbar_init(&S.full[1], 1);
-        for (int k = 0; k < kIxSlots; k++) {
+        for (int k = 0; k < 2; k++) {
             mbar_init(&S.pub[k], 1);
             mbar_init(&S.lb[k], 1);
-            S.cnt[k] = 0;
         }
+        for (int k = 0; k < kIxSlots; k++) S.cnt[k] = 0;
         S.issued[0] = S.issued[1] = S.used[0] = S.used[1] = 0;
         S.stop = 0;
         fence_mbar_init();
-        for (uint32_t i = 0; i < 2 && i < own; i++) ix_issue(p, S, blockIdx.x + i * G, (int)i);
+        if (own > 0) {
+            const uint32_t g = blockIdx.x;
+            for (int k = 0; k < tiles_of(g); k++) ix_issue(p, S, g * kIxGroup + k, k);
+        }
     }
     __syncthreads();
     if (warp >= kIxSched) {
-        // ---- scheduler warp: the look-backs, in tile order
+        // ---- scheduler warp: the look-backs, in group order
         for (uint32_t j = (uint32_t)(warp - kIxSched); j < own; j += kIxScheds) {
-            const int rs = (int)(j % kIxSlots);
-            // the look-back starts once this CTA's own tile is published, by
-            // which time the tiles before it in the round mostly are too
+            const uint32_t g = blockIdx.x + j * G;
+            const int gs = (int)(j & 1);
+            // the look-back starts once this CTA's own group is published, by
+            // which time the groups before it in the round mostly are too
             // (starting earlier only adds polling traffic)
-            const bool pub_ok = mbar_wait(&S.pub[rs], (j / kIxSlots) & 1, kWaitNs);
+            const bool pub_ok = mbar_wait(&S.pub[gs], (j >> 1) & 1, kWaitNs);
             uint32_t entry = 0, bs = 0, bt = 0;
-            const bool lb_ok = __all_sync(0xffffffffu, pub_ok) &&
-                               ix_lookback<D>(p, st, blockIdx.x + j * G, lane, entry, bs, bt);
+            const bool lb_ok = __all_sync(0xffffffffu, pub_ok) && ix_lookback<D>(p, st, g, lane, entry, bs, bt);
             const bool ok = pub_ok && lb_ok;
             if (!__all_sync(0xffffffffu, ok) || ix_stopped(S)) {
                 if (lane == 0) {
                     if (!pub_ok) fail(p.hdr, ERR_TIMEOUT);
                     ix_set_stop(S);
-                    mbar_arrive(&S.lb[rs]);  // the compute warps see stop
+                    mbar_arrive(&S.lb[gs]);  // the compute warps see stop
                 }
                 break;
             }
-            ix_place<D>(p, S, st, blockIdx.x + j * G, rs, lane, entry, bs, bt);
+            // each tile of the group: entry state and offsets, in order
+            const int nt = tiles_of(g);
+            uint32_t s = entry, cs = bs, ct = bt;
+            for (int k = 0; k < nt; k++) {
+                const int slot = 2 * gs + k;
+                const uint32_t tot = ix_place<D>(S, slot, lane, s, cs, ct);
+                s = fb_apply(S.tf[slot], s);
+                cs += tot & 0xFFFFu;
+                ct += tot >> 16;
+            }
+            if (lane == 0) {
+                IxStatus *me = st + g;
+                me->exit = s;
+                me->incl_s = cs;
+                me->incl_t = ct;
+                st_release(&me->flag, p.epoch * 4 + 2);
+                if (g == groups - 1) {
+                    p.hdr->n_struct = cs;
+                    p.hdr->n_terms = ct;
+                }
+            }
             __syncwarp();
-            if (lane == 0) mbar_arrive(&S.lb[rs]);
+            if (lane == 0) mbar_arrive(&S.lb[gs]);
         }
     } else {
-        // ---- compute warps: local pass of tile i, output of tile i - kIxSlots + 1
-        for (uint32_t i = 0; i < own + kIxSlots - 1; i++) {
+        // ---- compute warps: local passes of group i, output of group i - 1
+        for (uint32_t i = 0; i < own + 1; i++) {
+            bool quit = false;
             if (i < own) {
-                const uint32_t tile = blockIdx.x + i * G;
-                const int bs = (int)(i & 1), rs = (int)(i % kIxSlots);
-                const bool ok = mbar_wait(&S.full[bs], (i >> 1) & 1, kWaitNs);
-                // the abort flag is read every 16th tile: every wait is bounded
-                const bool ab = lane == 0 && (i & 15) == 15 && aborted(p.hdr);
-                if (!__all_sync(0xffffffffu, ok) || __any_sync(0xffffffffu, ab) || ix_stopped(S)) {
-                    if (lane == 0) {
-                        if (!ok) fail(p.hdr, ERR_TMA);
-                        ix_set_stop(S);
-                    }
-                    break;
-                }
-                ix_local<D>(p, S, tile, bs, rs);
-                __syncwarp();
-                uint32_t last = 0;
-                if (lane == 0) {
-                    __threadfence_block();  // this warp's shared-memory results before the count
-                    last = atomicAdd(&S.cnt[rs], 1u) == kWarps - 1;
-                }
-                if (__shfl_sync(0xffffffffu, last, 0)) {
-                    __threadfence_block();  // every warp's results are visible to the last one
-                    ix_publish<D>(p, S, st, tile, rs, lane);
-                    if (lane == 0) {
-                        S.cnt[rs] = 0;
-                        S.used[bs]++;
-                        // every warp has read buf[bs]: refill it with the tile after next
-                        if (i + 2 < own) {
-                            fence_proxy_async();
-                            ix_issue(p, S, tile + 2 * G, bs);
+                const uint32_t g = blockIdx.x + i * G;
+                const int gs = (int)(i & 1), nt = tiles_of(g);
+                for (int k = 0; k < nt && !quit; k++) {
+                    const uint32_t tile = g * kIxGroup + k;
+                    const int rs = 2 * gs + k;
+                    const bool ok = mbar_wait(&S.full[k], i & 1, kWaitNs);
+                    // the abort flag is read every 16th group: every wait is bounded
+                    const bool ab = lane == 0 && k == 0 && (i & 15) == 15 && aborted(p.hdr);
+                    if (!__all_sync(0xffffffffu, ok) || __any_sync(0xffffffffu, ab) || ix_stopped(S)) {
+                        if (lane == 0) {
+                            if (!ok) fail(p.hdr, ERR_TMA);
+                            ix_set_stop(S);
                         }
-                        mbar_arrive(&S.pub[rs]);
+                        quit = true;
+                        break;
+                    }
+                    ix_local<D>(p, S, tile, k, rs);
+                    __syncwarp();
+                    uint32_t last = 0;
+                    if (lane == 0) {
+                        __threadfence_block();  // this warp's shared-memory results before the count
+                        last = atomicAdd(&S.cnt[rs], 1u) == kWarps - 1;
+                    }
+                    if (__shfl_sync(0xffffffffu, last, 0)) {
+                        __threadfence_block();  // every warp's results are visible to the last one
+                        ix_tile_agg<D>(S, rs, lane);
+                        if (lane == 0) {
+                            S.cnt[rs] = 0;
+                            S.used[k]++;
+                            // every warp has read buf[k]: refill it with tile k of
+                            // this CTA's next group
+                            if (i + 1 < own) {
+                                const uint32_t g2 = g + G;
+                                if (k < tiles_of(g2)) {
+                                    fence_proxy_async();
+                                    ix_issue(p, S, g2 * kIxGroup + k, k);
+                                }
+                            }
+                            if (k == nt - 1) {
+                                ix_group_publish<D>(p, S, st, g, 2 * gs, nt);
+                                mbar_arrive(&S.pub[gs]);
+                            }
+                        }
                     }
                 }
             }
-            if (i + 1 >= kIxSlots) {
-                const uint32_t o = i + 1 - kIxSlots;  // tile whose output is due
-                const int rs = (int)(o % kIxSlots);
-                const bool ok = mbar_wait(&S.lb[rs], (o / kIxSlots) & 1, kWaitNs);
+            if (quit) break;
+            if (i >= 1) {
+                const uint32_t o = i - 1;  // group whose output is due
+                const uint32_t g = blockIdx.x + o * G;
+                const int gs = (int)(o & 1);
+                const bool ok = mbar_wait(&S.lb[gs], (o >> 1) & 1, kWaitNs);
                 if (!__all_sync(0xffffffffu, ok) || ix_stopped(S)) {
                     if (lane == 0 && !ok) {
                         fail(p.hdr, ERR_TIMEOUT);
@@ -702,7 +761,8 @@ __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_
                     }
                     break;
                 }
-                ix_output<D>(p, S, blockIdx.x + o * G, rs);
+                const int nt = tiles_of(g);
+                for (int k = 0; k < nt; k++) ix_output<D>(p, S, g * kIxGroup + k, 2 * gs + k);
             }
         }
     }
