@@ -801,6 +801,8 @@ def bench_speculation(eng, args):
         "speculative": {"value": round(gib / (t_spec / 1e3), 3), "unit": "GiB/s", "ms": round(t_spec, 4),
                         "predict_ms": round(t_pred, 4)},
         "speedup_vs_plain": round(t_plain / t_spec, 4),
+        "speedup_vs_constant_guess": round(t_const / t_spec, 4),
+        "plain_kernel": "index_pass_kernel (groups of two tiles); the speculative scan runs on the tile kernel",
         "constant_guess": {"value": round(gib / (t_const / 1e3), 3), "unit": "GiB/s",
                            "mispredicted_tiles": int(wrong_const)},
         "tiles": int(tiles), "mispredicted_tiles": int(wrong), "misprediction_rate": round(wrong / max(tiles, 1), 6),

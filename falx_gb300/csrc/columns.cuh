@@ -179,6 +179,13 @@ __device__ __forceinline__ void copy_staged(const uint8_t *sd, uint32_t o, uint3
     for (; i < n; i++) dst[i] = sd[o + i];
 }
 
+// A string cell outside the staged window, cleaned into the arena (out of
+// line: rare, and the cell loop is instruction-fetch bound).
+__device__ __noinline__ void copy_unstaged(const uint8_t *src, uint32_t n, uint8_t *arena, uint32_t pos,
+                                           uint64_t cap) {
+    copy_clean(src, n, arena, pos, cap);
+}
+
 // Select from a small per-thread array by a warp-uniform slot without
 // dynamic register indexing (which would move the array to local memory).
 template <typename T, int N>
@@ -199,11 +206,6 @@ struct Slow64 {
     uint64_t v;
     bool ok;
 };
-__device__ __noinline__ Slow64 slow_i64(const uint8_t *s, uint32_t n) {
-    int64_t v = 0;
-    const bool ok = dec::numeric_view(s, n) && dec::parse_i64(s, n, v);
-    return {(uint64_t)v, ok};
-}
 __device__ __noinline__ Slow64 slow_u32(const uint8_t *s, uint32_t n) {
     uint32_t v = 0;
     const bool ok = dec::numeric_view(s, n) && dec::parse_u32(s, n, v);
@@ -213,6 +215,15 @@ __device__ __noinline__ Slow64 slow_f64(const uint8_t *s, uint32_t n) {
     double v = 0;
     const bool ok = dec::numeric_view(s, n) && dec::parse_f64(s, n, v);
     return {dec::d2u(v), ok};
+}
+// An i64 cell: 1-8 plain digits word at a time when staged, else the full
+// decoder.
+__device__ __noinline__ Slow64 i64_cell(const uint8_t *sd, bool staged, uint32_t o, const uint8_t *s, uint32_t n) {
+    uint32_t u;
+    if (staged && swar_u32(sd, o, n, u)) return {u, true};
+    int64_t v = 0;
+    const bool ok = dec::numeric_view(s, n) && dec::parse_i64(s, n, v);
+    return {(uint64_t)v, ok};
 }
 // One count / sum cell: whether it is a value, its bits, and its exact
 // x1e6 value when it has one.
@@ -725,7 +736,7 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
                     quoted = n >= 2 && src[0] == '"' && src[n - 1] == '"';
                     if (!quoted) {
                         if (W.staged(a, n, o) && (uint64_t)pos + n <= rs.str_cap[c]) copy_staged(W.sdata, o, n, arena + pos);
-                        else copy_clean(src, n, arena, pos, rs.str_cap[c]);
+                        else copy_unstaged(src, n, arena, pos, rs.str_cap[c]);
                         len = n;
                     }
                 }
@@ -769,17 +780,11 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
                 }
                 if (store) static_cast<uint64_t *>(rs.values[c])[g] = ok ? bits : 0ull;
             } else if (ty == 0) {
-                int64_t v = 0;
-                uint32_t u;
-                if (present) {
-                    if (st && swar_u32(W.sdata, o, n, u)) v = u;
-                    else {
-                        const Slow64 r = slow_i64(W.ptr(a, n), n);
-                        v = (int64_t)r.v;
-                        ok = r.ok;
-                    }
-                }
-                if (store) static_cast<int64_t *>(rs.values[c])[g] = ok ? v : 0;
+                // out of line: the cell loop is instruction-fetch bound, and
+                // i64 columns are rarer than u32 / f64 / str
+                const Slow64 r = present ? i64_cell(W.sdata, st, o, W.ptr(a, n), n) : Slow64{0, false};
+                ok = r.ok;
+                if (store) static_cast<int64_t *>(rs.values[c])[g] = ok ? (int64_t)r.v : 0;
             } else {
                 ok = present && n > 0;
                 if (store) {
