@@ -857,7 +857,7 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
 // written to (the index pass bounds its writes) flags ERR_TAPE and the host
 // runs both passes again with buffers of the exact size.
 template <int D, bool STATS>
-__global__ void __launch_bounds__(kThreads, 4) columns_kernel(const __grid_constant__ ColParams p) {
+__global__ void __launch_bounds__(kThreads, 3) columns_kernel(const __grid_constant__ ColParams p) {
     extern __shared__ __align__(16) uint8_t col_smem_raw[];
     ColSmem &S = *reinterpret_cast<ColSmem *>(col_smem_raw);
     const int tid = threadIdx.x;
