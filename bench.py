@@ -366,10 +366,21 @@ def bench_gpu(args):
         e2e_step()
         e2e_t.append(time.perf_counter() - s)
     e2e_s = float(np.median(e2e_t))
+    # the same calls without the pipeline: one copy in, the parse, the copies back
+    eng.lib.falx_set_option(eng.ctx, _lib.OPT_PIPELINE, 0)
+    whole_t = []
+    for _ in range(3):
+        s = time.perf_counter()
+        e2e_step()
+        whole_t.append(time.perf_counter() - s)
+    eng.lib.falx_set_option(eng.ctx, _lib.OPT_PIPELINE, 1)
     d2h = 4 * n_struct + rows * (4 + 4 + 8 + 8) + 5 * words * 8 + 4 * (rows + 1) + str_len
     e2e = {"value": round(n / GIB / e2e_s, 4), "unit": "GiB/s", "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
            "ms_per_step": round(e2e_s * 1e3, 3), "ms_min_max": [round(min(e2e_t) * 1e3, 3), round(max(e2e_t) * 1e3, 3)],
-           "calls": len(e2e_t)}
+           "calls": len(e2e_t),
+           "form": "pipelined: 8 input chunks, each copied in, parsed and copied back while the others move",
+           "whole_input": {"value": round(n / GIB / float(np.median(whole_t)), 4), "unit": "GiB/s",
+                           "ms_per_step": round(float(np.median(whole_t)) * 1e3, 3)}}
 
     # The step's outputs, copied back once after timing, for the parity check.
     gpu_out = None

@@ -156,6 +156,7 @@ SIGNATURES = {
 OPT_ROWS_PATH = 1
 OPT_CTAS_PER_SM = 2
 OPT_TIMING = 3
+OPT_PIPELINE = 4
 MLP_BYTES = 256
 SPEC_TILE = 16384
 

@@ -57,6 +57,18 @@ struct ColParams {
     uint32_t blk0;     // first record block of the launch (ticket k runs block blk0 + k)
     uint64_t wait_ns;  // look-back wait limit
     DevHeader *hdr;
+    // Launches over consecutive chunks of one input (pipelined host-buffer
+    // calls): the tape counts through this chunk come from seed_hi[1..2]
+    // (written by the chunk's index pass) instead of the header; the launch
+    // takes the record blocks that end before the chunk's last terminator
+    // (all the rest when `last`), from its own ticket, and its last block
+    // writes the rows and arena bytes through it to chunk_out[0..4]
+    // (chunk_out[5] = 1 once written).
+    const uint32_t *seed_lo;  // the previous chunk's seed record, NULL for the first chunk
+    const uint32_t *seed_hi;
+    uint32_t *ticket;
+    unsigned long long *chunk_out;
+    uint32_t last;
     RowSpec rows;
 };
 
@@ -68,7 +80,8 @@ struct ColParams {
 struct TapeCounts {
     uint64_t n_seps, n_ends;
     uint64_t n_recs;    // n_ends, plus one for a trailing record without terminator
-    uint32_t n_blocks;  // record blocks
+    uint32_t n_blocks;  // record blocks: this launch takes [blk_lo, n_blocks)
+    uint32_t blk_lo;
 };
 
 struct ColSmem {
@@ -644,6 +657,12 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
                 p.hdr->n_rows = pre[0] + tot[0];
 #pragma unroll
                 for (int k = 0; k < kMaxStr; k++) p.hdr->arena[k] = pre[1 + k] + tot[1 + k];
+                if (p.chunk_out) {
+                    p.chunk_out[0] = pre[0] + tot[0];
+#pragma unroll
+                    for (int k = 0; k < kMaxStr; k++) p.chunk_out[1 + k] = pre[1 + k] + tot[1 + k];
+                    p.chunk_out[5] = 1;
+                }
             }
         }
         if (lane == 0)
@@ -862,16 +881,25 @@ __global__ void __launch_bounds__(kThreads, 3) columns_kernel(const __grid_const
     ColSmem &S = *reinterpret_cast<ColSmem *>(col_smem_raw);
     const int tid = threadIdx.x;
     TapeCounts tc;
-    tc.n_ends = *(volatile const unsigned long long *)&p.hdr->n_terms;
-    tc.n_seps = *(volatile const unsigned long long *)&p.hdr->n_struct - tc.n_ends;
+    if (p.seed_hi) {
+        tc.n_ends = p.seed_hi[2];
+        tc.n_seps = (uint64_t)p.seed_hi[1] - p.seed_hi[2];
+    } else {
+        tc.n_ends = *(volatile const unsigned long long *)&p.hdr->n_terms;
+        tc.n_seps = *(volatile const unsigned long long *)&p.hdr->n_struct - tc.n_ends;
+    }
     tc.n_recs = tc.n_ends + 1;
     tc.n_blocks = (uint32_t)((tc.n_recs + kRecBlock - 1) / kRecBlock);
+    tc.blk_lo = 0;
+    if (p.seed_hi && !p.last) tc.n_blocks = (uint32_t)(tc.n_ends / kRecBlock);  // blocks whose records all end here
+    if (p.seed_lo) tc.blk_lo = p.seed_lo[2] / kRecBlock;  // the previous chunk's launch took the blocks before
     if (tc.n_seps > p.seps_cap || tc.n_ends > p.ends_cap) {
         if (tid == 0 && blockIdx.x == 0) atomicOr(&p.hdr->error, ERR_TAPE);
         return;
     }
+    unsigned int *ticket = p.ticket ? p.ticket : &p.hdr->col_ticket;
     for (;;) {
-        if (tid == 0) S.blk = p.blk0 + atomicAdd(&p.hdr->col_ticket, 1u);
+        if (tid == 0) S.blk = tc.blk_lo + p.blk0 + atomicAdd(ticket, 1u);
         __syncthreads();  // also: the previous block is done with shared memory
         const uint32_t blk = S.blk;
         if (blk >= tc.n_blocks) break;

@@ -77,6 +77,15 @@ struct falx_ctx {
     uint32_t col_epoch = 0;         // their tag
     uint64_t stall_test_ns = 0;     // falx_test_stalled_lookback
     int col_grid[5][2] = {};        // persistent columns grid per dialect, without / with the count-sum sink
+    // pipelined host-buffer parse: input chunks copied in, parsed and their
+    // outputs copied out while the next chunks are still on their way
+    int pipeline = 1;               // FALX_OPT_PIPELINE
+    const void *pipe = nullptr;     // the call's host buffers while one runs (falx_parse_host)
+    bool pipe_done = false;         // the outputs were copied back chunk by chunk
+    cudaStream_t out_stream = nullptr;
+    uint32_t *pipe_dev = nullptr;   // seed records, tickets and per-chunk totals
+    unsigned long long *pipe_host = nullptr;  // pinned copies of the seed records and per-chunk totals
+    cudaEvent_t pipe_ev[32] = {};   // per chunk: input landed, results ready
     // bgzf inflate: block table, per-block status and failure count
     void *gz_scratch = nullptr;
     uint64_t gz_cap = 0;

@@ -622,13 +622,14 @@ bool valid_dialect(int d) { return d >= FALX_CSV && d <= FALX_NDJSON; }
 
 // Launch the scan over [data, data+len) with the outputs in `P` (device);
 // the header (counts, error bits) is final once the stream reaches this point.
-int launch_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t len, Params P, bool spec = false) {
+int launch_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64_t len, Params P, bool spec = false,
+                bool keep_hdr = false) {
     uint64_t shift = (uint64_t)((uintptr_t)data & 15u);
     uint64_t tiles64 = (len + shift + kTile - 1) / kTile;
     uint32_t tiles = (uint32_t)tiles64;
     int rc = ensure_status(c, tiles);
     if (rc) return rc;
-    FALX_CUDA(cudaMemsetAsync(c->hdr, 0, sizeof(DevHeader), c->stream));
+    if (!keep_hdr) FALX_CUDA(cudaMemsetAsync(c->hdr, 0, sizeof(DevHeader), c->stream));
     P.data = data;
     P.abase = data - shift;
     P.len = len;
@@ -878,6 +879,216 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     return FALX_OK;
 }
 
+// Host buffers of a pipelined falx_parse_host call.
+struct HostPipe {
+    const uint8_t *in;      // the input (host)
+    const falx_outputs *ho;  // the caller's host outputs
+    const falx_schema *schema;
+};
+
+constexpr int kPipeChunks = 8;
+constexpr int kPipeRetry = 1;  // the tape outgrew its scratch: run the whole-input path instead
+
+// Rows of a host-buffer call as a pipeline over kPipeChunks input chunks
+// (whole tiles each): copy stream H2D chunk k; compute stream: index pass
+// over chunk k seeded from chunk k - 1's exit state and counts (device
+// records, no host round trip), columns kernel over the record blocks that
+// end inside chunks 0..k; out stream: chunk k's index, tape, column values,
+// offsets, arena and full validity words copied back once the host sees
+// chunk k's totals. The tape and the look-back records of the columns pass
+// are shared by all launches, so outputs are those of one whole-input call.
+int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len, Params P, const HostPipe &hp) {
+    const RowSpec rs = P.rows;
+    memset(&P.rows, 0, sizeof P.rows);
+    c->last_n = 0;
+    const falx_outputs *ho = hp.ho;
+    const falx_columns *hc = ho->columns;
+    if (!c->copy_stream) FALX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    if (!c->out_stream) FALX_CUDA(cudaStreamCreateWithFlags(&c->out_stream, cudaStreamNonBlocking));
+    if (!c->in_free) FALX_CUDA(cudaEventCreateWithFlags(&c->in_free, cudaEventDisableTiming));
+    for (int k = 0; k < 2 * kPipeChunks; k++)
+        if (!c->pipe_ev[k]) FALX_CUDA(cudaEventCreateWithFlags(&c->pipe_ev[k], cudaEventDisableTiming));
+    // device: seed records (kPipeChunks + 1) x 3 u32 | tickets | per-chunk totals 6 u64 each
+    constexpr size_t kSeedB = (kPipeChunks + 1) * 3 * 4, kTickB = kPipeChunks * 4, kOutB = kPipeChunks * 6 * 8;
+    constexpr size_t kPipeB = 512 + kOutB;
+    static_assert(kSeedB + kTickB <= 512, "pipeline records");
+    if (!c->pipe_dev) FALX_CUDA(cudaMalloc(&c->pipe_dev, kPipeB));
+    if (!c->pipe_host) FALX_CUDA(cudaHostAlloc(&c->pipe_host, kPipeB, cudaHostAllocDefault));
+    uint32_t *seeds = c->pipe_dev;
+    uint32_t *tickets = c->pipe_dev + (kPipeChunks + 1) * 3;
+    unsigned long long *chunk_out = reinterpret_cast<unsigned long long *>(reinterpret_cast<uint8_t *>(c->pipe_dev) + 512);
+    const uint32_t *h_seeds = reinterpret_cast<const uint32_t *>(c->pipe_host);
+    const unsigned long long *h_out = c->pipe_host + 64;
+    // chunks of whole tiles (the device input is 256-byte aligned)
+    const uint64_t tiles = (len + kTile - 1) / kTile;
+    const uint64_t ct = (tiles + kPipeChunks - 1) / kPipeChunks;
+    const int nk = (int)((tiles + ct - 1) / ct);
+    auto off = [&](int k) { return std::min(len, (uint64_t)k * ct * kTile); };
+    // tape scratch sized from the input; a tape that outgrows it sends the
+    // call to the whole-input path
+    const uint64_t want_seps = (len / 6 + 1024) * 4, want_ends = (len / 24 + 1024) * 8;
+    int rc = grow_scratch((void **)&c->tape_seps, &c->tape_seps_cap, want_seps);
+    if (!rc) rc = grow_scratch((void **)&c->tape_ends, &c->tape_ends_cap, want_ends);
+    if (rc) return rc;
+    P.seps = c->tape_seps;
+    P.seps_cap = c->tape_seps_cap / 4;
+    P.ends = c->tape_ends;
+    P.ends_cap = c->tape_ends_cap / 8;
+    const uint64_t blocks = (P.ends_cap + 1 + kRecBlock - 1) / kRecBlock;
+    if (blocks * sizeof(BlkStatus) > c->rec_sums_cap || c->col_epoch >= (1u << 29)) {
+        rc = grow_scratch(&c->rec_sums, &c->rec_sums_cap, blocks * sizeof(BlkStatus));
+        if (rc) return rc;
+        FALX_CUDA(cudaMemsetAsync(c->rec_sums, 0, c->rec_sums_cap, c->stream));
+        c->col_epoch = 0;
+    }
+    const uint32_t col_epoch = ++c->col_epoch;
+    FALX_CUDA(cudaMemsetAsync(c->hdr, 0, sizeof(DevHeader), c->stream));
+    FALX_CUDA(cudaMemsetAsync(c->pipe_dev, 0, kPipeB, c->stream));
+    // the input buffer is overwritten only after earlier work on the stream
+    FALX_CUDA(cudaEventRecord(c->in_free, c->stream));
+    FALX_CUDA(cudaStreamWaitEvent(c->copy_stream, c->in_free, 0));
+    for (int k = 0; k < nk; k++) {
+        FALX_CUDA(cudaMemcpyAsync(const_cast<uint8_t *>(dev_in) + off(k), hp.in + off(k), off(k + 1) - off(k),
+                                  cudaMemcpyHostToDevice, c->copy_stream));
+        FALX_CUDA(cudaEventRecord(c->pipe_ev[k], c->copy_stream));
+    }
+    for (int k = 0; k < nk; k++) {
+        FALX_CUDA(cudaStreamWaitEvent(c->stream, c->pipe_ev[k], 0));
+        Params Pk = P;
+        Pk.seeded = k > 0;
+        Pk.prev_byte = k > 0 ? hp.in[off(k) - 1] : 0u;
+        Pk.entry0 = 0;
+        Pk.pos_base = off(k);
+        Pk.sep_base = 0;
+        Pk.seed_in = k > 0 ? seeds + 3 * k : nullptr;
+        Pk.seed_out = seeds + 3 * (k + 1);
+        rc = launch_scan(c, dialect, false, dev_in + off(k), off(k + 1) - off(k), Pk, false, true);
+        if (rc) return rc;
+        ColParams cp;
+        memset(&cp, 0, sizeof cp);
+        cp.data = dev_in;
+        cp.abase = dev_in;
+        cp.len = len;
+        cp.seps = P.seps;
+        cp.seps_cap = P.seps_cap;
+        cp.ends = P.ends;
+        cp.ends_cap = P.ends_cap;
+        cp.hdr = c->hdr;
+        cp.rows = rs;
+        cp.status = static_cast<BlkStatus *>(c->rec_sums);
+        cp.epoch = col_epoch;
+        cp.wait_ns = kWaitNs;
+        cp.seed_lo = k > 0 ? seeds + 3 * k : nullptr;
+        cp.seed_hi = seeds + 3 * (k + 1);
+        cp.ticket = tickets + k;
+        cp.chunk_out = chunk_out + 6 * k;
+        cp.last = k == nk - 1;
+#define FALX_COLS(D)                                                                                        \
+    do {                                                                                                    \
+        rc = rs.want_stats ? columns_grid<D, true>(c) : columns_grid<D, false>(c);                          \
+        if (rc) return rc;                                                                                  \
+        const unsigned grid_ = (unsigned)c->col_grid[D][rs.want_stats ? 1 : 0];                             \
+        if (rs.want_stats) columns_kernel<D, true><<<grid_, kThreads, sizeof(ColSmem), c->stream>>>(cp);   \
+        else columns_kernel<D, false><<<grid_, kThreads, sizeof(ColSmem), c->stream>>>(cp);                \
+    } while (0)
+        switch (dialect) {
+        case FALX_CSV: FALX_COLS(D_CSV); break;
+        case FALX_CSV_HASH: FALX_COLS(D_CSV_HASH); break;
+        case FALX_TSV: FALX_COLS(D_TSV); break;
+        default: FALX_COLS(D_LOGFMT); break;
+        }
+#undef FALX_COLS
+        FALX_CUDA(cudaGetLastError());
+        FALX_CUDA(cudaMemcpyAsync(c->pipe_host, seeds, kSeedB, cudaMemcpyDeviceToHost, c->stream));
+        FALX_CUDA(cudaMemcpyAsync(c->pipe_host + 64, chunk_out, kOutB, cudaMemcpyDeviceToHost, c->stream));
+        FALX_CUDA(cudaEventRecord(c->pipe_ev[kPipeChunks + k], c->stream));
+    }
+    // copy each chunk's outputs back as soon as its totals are in
+    uint64_t ps = 0, pt = 0, prow = 0, pw = 0, poff = 0, parena[kMaxStr] = {0, 0, 0, 0};
+    auto back = [&](void *dst, const void *src, uint64_t bytes) -> int {
+        if (bytes && dst) FALX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->out_stream));
+        return FALX_OK;
+    };
+    auto clampu = [](uint64_t v, uint64_t cap) { return v < cap ? v : cap; };
+    for (int k = 0; k < nk; k++) {
+        FALX_CUDA(cudaEventSynchronize(c->pipe_ev[kPipeChunks + k]));
+        const uint64_t s_k = h_seeds[3 * (k + 1) + 1], t_k = h_seeds[3 * (k + 1) + 2];
+        const bool wrote = h_out[6 * k + 5] != 0;
+        const uint64_t rows_k = wrote ? h_out[6 * k] : prow;
+        uint64_t arena_k[kMaxStr];
+        for (int j = 0; j < kMaxStr; j++) arena_k[j] = wrote ? h_out[6 * k + 1 + j] : parena[j];
+        if (ho->index && P.index) {
+            const uint64_t a = clampu(ps, ho->index_cap), b = clampu(s_k, ho->index_cap);
+            if (b > a && (rc = back(ho->index + a, P.index + a, (b - a) * 4))) return rc;
+        }
+        if (ho->seps && ho->seps_cap) {
+            const uint64_t a = clampu(ps - pt, ho->seps_cap), b = clampu(s_k - t_k, ho->seps_cap);
+            if (b > a && (rc = back(ho->seps + a, P.seps + a, (b - a) * 4))) return rc;
+        }
+        if (ho->ends && ho->ends_cap) {
+            const uint64_t a = clampu(pt, ho->ends_cap), b = clampu(t_k, ho->ends_cap);
+            if (b > a && (rc = back(ho->ends + a, P.ends + a, (b - a) * 8))) return rc;
+        }
+        if (hc) {
+            const uint64_t rcap = hc->rows_cap, wcap = (rcap + 63) / 64;
+            const uint64_t wk = clampu(rows_k / 64, wcap);
+            for (int j = 0; j < rs.ncols; j++) {
+                const uint32_t ty = rs.type[j];
+                const uint8_t *dv = static_cast<const uint8_t *>(rs.values[j]);
+                uint8_t *hv = static_cast<uint8_t *>(hc->cols[j].values);
+                if (ty == FALX_STR) {
+                    // offsets [0, rows_k] are final once a row exists (offset 0
+                    // is written by record block 0)
+                    const uint64_t a = clampu(poff, rcap + 1), b = rows_k ? clampu(rows_k + 1, rcap + 1) : a;
+                    if (b > a && (rc = back(hv + 4 * a, dv + 4 * a, (b - a) * 4))) return rc;
+                    const int sl = rs.str_slot[j];
+                    const uint64_t cap = hc->cols[j].str_cap;
+                    const uint64_t x = clampu(parena[sl], cap), y = clampu(arena_k[sl], cap);
+                    if (y > x && (rc = back(hc->cols[j].str_data + x, rs.str_data[j] + x, y - x))) return rc;
+                } else {
+                    const uint64_t es = ty == FALX_U32 ? 4 : 8;
+                    const uint64_t a = clampu(prow, rcap), b = clampu(rows_k, rcap);
+                    if (b > a && (rc = back(hv + es * a, dv + es * a, (b - a) * es))) return rc;
+                }
+                if (wk > pw && (rc = back(hc->cols[j].valid + pw, rs.valid[j] + pw, (wk - pw) * 8))) return rc;
+            }
+            pw = wk > pw ? wk : pw;
+            if (rows_k) poff = rows_k + 1;
+        }
+        ps = s_k;
+        pt = t_k;
+        prow = rows_k;
+        for (int j = 0; j < kMaxStr; j++) parena[j] = arena_k[j];
+    }
+    // the header (totals, errors), then the validity words not yet copied
+    FALX_CUDA(cudaMemcpyAsync(c->hhdr, c->hdr, sizeof(DevHeader), cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->hhdr->error & (ERR_TIMEOUT | ERR_TMA)) {
+        FALX_CUDA(cudaStreamSynchronize(c->out_stream));
+        return FALX_ERR_TIMEOUT;
+    }
+    if (c->hhdr->error & ERR_TAPE) {
+        FALX_CUDA(cudaStreamSynchronize(c->out_stream));
+        return kPipeRetry;
+    }
+    if (hc) {
+        const uint64_t wcap = (hc->rows_cap + 63) / 64;
+        const uint64_t wend = clampu((c->hhdr->n_rows + 63) / 64, wcap);
+        for (int j = 0; j < rs.ncols; j++) {
+            if (wend > pw && (rc = back(hc->cols[j].valid + pw, rs.valid[j] + pw, (wend - pw) * 8))) return rc;
+            // no rows at all: the string offsets array is the one 0
+            if (rs.type[j] == FALX_STR && poff == 0 && hc->rows_cap + 1 > 0 &&
+                (rc = back(hc->cols[j].values, rs.values[j], 4)))
+                return rc;
+        }
+    }
+    FALX_CUDA(cudaStreamSynchronize(c->out_stream));
+    c->pipe_done = true;
+    for (int k = 0; k < kMaxStr; k++)
+        if (c->hhdr->arena[k] > 0x7FFFFFFFull) return FALX_ERR_OVERFLOW;  // i32 string offsets
+    return FALX_OK;
+}
+
 // text_field: the City text lane's field (with o->stats: lat / lon), or
 // negative for none.
 int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, uint64_t len, falx_outputs *o,
@@ -937,8 +1148,14 @@ int parse_device(falx_ctx *c, const falx_schema *schema, const uint8_t *data, ui
         if (o->stats) memset(o->stats, 0, sizeof *o->stats);
         return FALX_OK;
     }
-    if (rows && (c->rows_path == 0 || rs.want_text)) rc = rows_two_pass(c, dialect, data, len, P);
-    else rc = run_scan(c, dialect, rows, data, len, P);
+    if (rows && c->pipe) {
+        rc = rows_pipelined(c, dialect, data, len, P, *static_cast<const HostPipe *>(c->pipe));
+        if (rc == kPipeRetry) return rc;
+    } else if (rows && (c->rows_path == 0 || rs.want_text)) {
+        rc = rows_two_pass(c, dialect, data, len, P);
+    } else {
+        rc = run_scan(c, dialect, rows, data, len, P);
+    }
     if (rc && rc != FALX_ERR_CAPACITY) return rc;  // on CAPACITY the counts are still reported
     const DevHeader &h = *c->hhdr;
     o->n_index = h.n_struct;
@@ -1045,6 +1262,11 @@ void falx_destroy(falx_ctx *c) {
     if (c->tape_ends) cudaFree(c->tape_ends);
     if (c->rec_sums) cudaFree(c->rec_sums);
     if (c->gz_scratch) cudaFree(c->gz_scratch);
+    if (c->pipe_dev) cudaFree(c->pipe_dev);
+    if (c->pipe_host) cudaFreeHost(c->pipe_host);
+    if (c->out_stream) cudaStreamDestroy(c->out_stream);
+    for (int k = 0; k < 32; k++)
+        if (c->pipe_ev[k]) cudaEventDestroy(c->pipe_ev[k]);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->arrive) cudaFree(c->arrive);
     if (c->in_free) cudaEventDestroy(c->in_free);
@@ -1063,6 +1285,10 @@ int falx_set_option(falx_ctx *c, int option, int value) {
     case FALX_OPT_CTAS_PER_SM:
         if (value < 0) return FALX_ERR_INVALID;
         c->ctas_per_sm = value;
+        return FALX_OK;
+    case FALX_OPT_PIPELINE:
+        if (value != 0 && value != 1) return FALX_ERR_INVALID;
+        c->pipeline = value;
         return FALX_OK;
     case FALX_OPT_TIMING:
         if (value && !c->ev[0])
@@ -1332,8 +1558,12 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     // Large inputs on the default rows path: copy in chunks on the copy
     // stream and let the index kernel start on the first chunk.
     const bool rows_call = hc || host_out->field_bytes || host_out->stats;
-    bool chunked = false, copied = false;
-    if (len >= kChunkedInMin && rows_call && c->rows_path == 0 && schema->dialect != FALX_NDJSON) {
+    // columns over a large input: the pipelined form (copies in and out
+    // overlap the parse, rows_pipelined)
+    const bool pipelined = c->pipeline && hc && len >= kChunkedInMin && c->rows_path == 0 &&
+                           schema->dialect != FALX_NDJSON;
+    bool chunked = false, copied = pipelined;
+    if (!pipelined && len >= kChunkedInMin && rows_call && c->rows_path == 0 && schema->dialect != FALX_NDJSON) {
         rc = start_chunked_input(c, host_data, len);
         if (rc < 0) return rc;
         chunked = rc == 1;
@@ -1354,13 +1584,26 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
         }
         d.columns = &dc;
     }
-    if (host_out->index_cap && host_out->index && hc) {
+    if (!pipelined && host_out->index_cap && host_out->index && hc) {
         if (!c->copy_stream) FALX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
         c->host_index = host_out->index;
         c->host_index_cap = host_out->index_cap;
         c->host_index_done = false;
     }
+    HostPipe hp{host_data, host_out, schema};
+    c->pipe = pipelined ? &hp : nullptr;
+    c->pipe_done = false;
     rc = parse_device(c, schema, c->dev_in, len, &d);
+    c->pipe = nullptr;
+    if (rc == kPipeRetry) {
+        // the tape outgrew the pipeline's scratch: the whole-input path on
+        // the input already in device memory (it sizes the tape exactly)
+        if (hc)
+            for (uint32_t k = 0; k < schema->ncols; k++) dc.cols[k].str_len = 0;
+        rc = parse_device(c, schema, c->dev_in, len, &d);
+    }
+    const bool pipe_done = c->pipe_done;
+    c->pipe_done = false;
     const bool index_done = c->host_index_done;
     c->host_index = nullptr;
     c->host_index_done = false;
@@ -1377,9 +1620,11 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     uint64_t ni = d.n_index < host_out->index_cap ? d.n_index : host_out->index_cap;
     uint64_t ns = d.n_seps < host_out->seps_cap ? d.n_seps : host_out->seps_cap;
     uint64_t ne = d.n_ends < host_out->ends_cap ? d.n_ends : host_out->ends_cap;
-    if (!r2 && !index_done) r2 = back(host_out->index, d.index, ni * 4);
-    if (!r2) r2 = back(host_out->seps, d.seps, ns * 4);
-    if (!r2) r2 = back(host_out->ends, d.ends, ne * 8);
+    if (!pipe_done) {  // (the pipeline copied every output back chunk by chunk)
+        if (!r2 && !index_done) r2 = back(host_out->index, d.index, ni * 4);
+        if (!r2) r2 = back(host_out->seps, d.seps, ns * 4);
+        if (!r2) r2 = back(host_out->ends, d.ends, ne * 8);
+    }
     if (hc) {
         falx_columns *ho = host_out->columns;
         uint64_t rows = dc.rows < hc->rows_cap ? dc.rows : hc->rows_cap;
@@ -1387,11 +1632,14 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
             uint32_t ty = schema->cols[k].type;
             uint64_t vb = ty == FALX_I64 || ty == FALX_F64 || ty == FALX_BYTES ? rows * 8
                           : ty == FALX_U32 ? rows * 4 : (rows + 1) * 4;
-            r2 = back(ho->cols[k].values, dc.cols[k].values, vb);
-            if (!r2) r2 = back(ho->cols[k].valid, dc.cols[k].valid, (rows + 63) / 64 * 8);
-            if (!r2 && ty == FALX_STR) {
-                uint64_t sl = dc.cols[k].str_len < hc->cols[k].str_cap ? dc.cols[k].str_len : hc->cols[k].str_cap;
-                r2 = back(ho->cols[k].str_data, dc.cols[k].str_data, sl);
+            if (!pipe_done) {
+                r2 = back(ho->cols[k].values, dc.cols[k].values, vb);
+                if (!r2) r2 = back(ho->cols[k].valid, dc.cols[k].valid, (rows + 63) / 64 * 8);
+                if (!r2 && ty == FALX_STR) {
+                    uint64_t sl =
+                        dc.cols[k].str_len < hc->cols[k].str_cap ? dc.cols[k].str_len : hc->cols[k].str_cap;
+                    r2 = back(ho->cols[k].str_data, dc.cols[k].str_data, sl);
+                }
             }
             ho->cols[k].str_len = dc.cols[k].str_len;
         }

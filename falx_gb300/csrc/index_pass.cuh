@@ -409,12 +409,13 @@ __device__ __forceinline__ void ix_group_publish(const Params &p, IxSmem &S, IxS
 // under the states they are entered in. No count vector per entry state is
 // carried.
 template <int D>
-__device__ __forceinline__ bool ix_lookback(const Params &p, IxStatus *st, uint32_t tile, int lane, uint32_t &entry,
-                                            uint32_t &bs, uint32_t &bt) {
+__device__ __forceinline__ bool ix_lookback(const Params &p, IxStatus *st, uint32_t tile, int lane, uint32_t e0,
+                                            uint32_t b0s, uint32_t b0t, uint32_t &entry, uint32_t &bs, uint32_t &bt) {
     constexpr int NS = NStates<D>::value;
-    entry = p.entry0;
-    bs = 0;
-    bt = 0;
+    // e0, b0s, b0t: the launch's entry state and the counts before it
+    entry = e0;
+    bs = b0s;
+    bt = b0t;
     if (tile > 0) {
         // ---- (1) the nearest inclusive prefix
         const uint64_t t0 = globaltimer_ns();
@@ -454,7 +455,7 @@ __device__ __forceinline__ bool ix_lookback(const Params &p, IxStatus *st, uint3
             }
         }
         fence_acq_rel_gpu();  // the relaxed flag loads above happen before the data loads below
-        uint32_t s = p.entry0;
+        uint32_t s = e0;
         if (jstar >= 0) {
             s = ld_relaxed(&st[jstar].exit);
             bs = ld_relaxed(&st[jstar].incl_s);
@@ -655,6 +656,8 @@ __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_
     __syncthreads();
     if (warp >= kIxSched) {
         // ---- scheduler warp: the look-backs, in group order
+        const uint32_t e0 = p.seed_in ? p.seed_in[0] : p.entry0;
+        const uint32_t b0s = p.seed_in ? p.seed_in[1] : 0u, b0t = p.seed_in ? p.seed_in[2] : 0u;
         for (uint32_t j = (uint32_t)(warp - kIxSched); j < own; j += kIxScheds) {
             const uint32_t g = blockIdx.x + j * G;
             const int gs = (int)(j & 1);
@@ -663,7 +666,8 @@ __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_
             // (starting earlier only adds polling traffic)
             const bool pub_ok = mbar_wait(&S.pub[gs], (j >> 1) & 1, kWaitNs);
             uint32_t entry = 0, bs = 0, bt = 0;
-            const bool lb_ok = __all_sync(0xffffffffu, pub_ok) && ix_lookback<D>(p, st, g, lane, entry, bs, bt);
+            const bool lb_ok =
+                __all_sync(0xffffffffu, pub_ok) && ix_lookback<D>(p, st, g, lane, e0, b0s, b0t, entry, bs, bt);
             const bool ok = pub_ok && lb_ok;
             if (!__all_sync(0xffffffffu, ok) || ix_stopped(S)) {
                 if (lane == 0) {
@@ -692,6 +696,11 @@ __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_
                 if (g == groups - 1) {
                     p.hdr->n_struct = cs;
                     p.hdr->n_terms = ct;
+                    if (p.seed_out) {
+                        p.seed_out[0] = s;
+                        p.seed_out[1] = cs;
+                        p.seed_out[2] = ct;
+                    }
                 }
             }
             __syncwarp();

@@ -89,6 +89,13 @@ struct Params {
     const uint32_t *arrive;
     uint32_t arrive_tag;
     uint32_t chunk_tiles;
+    // Index-pass launches over consecutive chunks of one input (pipelined
+    // host-buffer calls): the entry state and the structurals / terminators
+    // before the chunk are read from seed_in[0..2] (written by the previous
+    // chunk's launch), and the chunk's last group writes its exit state and
+    // the totals through the chunk to seed_out[0..2].
+    const uint32_t *seed_in;
+    uint32_t *seed_out;
     RowSpec rows;
 };
 

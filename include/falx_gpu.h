@@ -72,6 +72,13 @@ void falx_destroy(falx_ctx *ctx);
 #define FALX_OPT_ROWS_PATH 1
 #define FALX_OPT_CTAS_PER_SM 2
 #define FALX_OPT_TIMING 3 /* 1: time each launch of the rows path with CUDA events */
+/* FALX_OPT_PIPELINE (default 1): falx_parse_host with columns over 64 MiB or
+ * more runs as a pipeline of eight input chunks: each chunk is copied in,
+ * indexed and its records decoded while later chunks are still being copied
+ * in, and its outputs are copied back while later chunks are parsed (host to
+ * device and device to host transfers overlap). 0: one copy in, the whole
+ * parse, the copies back. Same outputs either way. */
+#define FALX_OPT_PIPELINE 4
 int falx_set_option(falx_ctx *ctx, int option, int value);
 /* Device times (ms) of the last rows call's launches, in order: index + tape,
  * columns. Returns how many were recorded (0 unless FALX_OPT_TIMING is on

@@ -1,6 +1,8 @@
 """Host-buffer entry point (falx_parse_host): input copied in, index and
-columns copied back (the index on its own stream while the columns kernel
-runs), checked against the oracle."""
+columns copied back, checked against the oracle. Inputs of 64 MiB and more
+with columns run as a pipeline of input chunks (copies in and out overlap
+the parse); the whole-input form (FALX_OPT_PIPELINE 0) must give the same
+outputs."""
 
 import ctypes
 
@@ -16,7 +18,7 @@ pytestmark = pytest.mark.gpu
 COLS = [(0, fx.U32), (1, fx.STR), (3, fx.U32), (4, fx.F64), (5, fx.F64)]
 
 
-def parse_host(engine, doc, dialect, cols):
+def parse_host(engine, doc, dialect, cols, tape=False):
     n = len(doc)
     src = np.frombuffer(doc, dtype=np.uint8).copy() if n else np.zeros(1, dtype=np.uint8)
     idx_cap, rows_cap, str_cap = n // 2 + 64, n // 2 + 64, n + 64
@@ -41,10 +43,20 @@ def parse_host(engine, doc, dialect, cols):
     out.index = index.ctypes.data
     out.index_cap = idx_cap
     out.columns = ctypes.pointer(hcols)
+    fb = _lib.falx_field_byte_stats()
+    out.field_bytes = ctypes.pointer(fb)
+    if tape:
+        seps = np.zeros(n + 64, dtype=np.uint32)
+        ends = np.zeros(n // 2 + 64, dtype=np.uint64)
+        out.seps, out.seps_cap = seps.ctypes.data, seps.size
+        out.ends, out.ends_cap = ends.ctypes.data, ends.size
     cs = fx.Schema(dialect, cols).to_c()
     _lib.check(engine.lib.falx_parse_host(engine.ctx, ctypes.byref(cs), ctypes.c_void_p(src.ctypes.data), n,
                                           ctypes.byref(out)), "falx_parse_host")
-    return index[: out.n_index], hcols.rows, keep, [hcols.cols[k].str_len for k in range(len(cols))]
+    res = (index[: out.n_index], hcols.rows, keep, [hcols.cols[k].str_len for k in range(len(cols))])
+    if tape:
+        return res + (seps[: out.n_seps], ends[: out.n_ends], (fb.fields, fb.bytes))
+    return res
 
 
 # 80 MiB and up: the input is copied in chunks and the index kernel starts
@@ -69,3 +81,42 @@ def test_parse_host_matches_oracle(engine, kind, dialect, size):
                 assert bytes(sd[: str_len[k]]) == want[k]["data"], (rep, k)
             else:
                 assert np.array_equal(v[:rows].view(np.uint8), np.asarray(want[k]["values"]).view(np.uint8)), (rep, k)
+
+
+def long_records_doc(n_target):
+    """Few, long records (about 200 KiB each): chunks of the pipeline that
+    hold no whole block of 512 records."""
+    rec = b"7," + b"x" * (200 << 10) + b',"a,b",3.5\n'
+    return rec * (n_target // len(rec) + 1)
+
+
+@pytest.mark.parametrize("kind,dialect,size", [(gen.CSV_HASH, fx.CSV_HASH, (100 << 20) + 7),
+                                               (gen.CSV_GEO, fx.CSV, 66 << 20),
+                                               (gen.ADVERSARIAL, fx.CSV_HASH, 70 << 20),
+                                               (None, fx.CSV, 70 << 20)])
+def test_pipelined_equals_whole_input(engine, kind, dialect, size):
+    doc = bytes(gen.generate(kind, size)) if kind is not None else long_records_doc(size)
+    doc = doc[:-1] if doc.endswith(b"\n") else doc  # a trailing record without terminator
+    cols = [(0, fx.U32), (1, fx.STR), (2, fx.F64)] if kind is None else COLS
+    got = parse_host(engine, doc, dialect, cols, tape=True)
+    engine.lib.falx_set_option(engine.ctx, _lib.OPT_PIPELINE, 0)
+    try:
+        want = parse_host(engine, doc, dialect, cols, tape=True)
+    finally:
+        engine.lib.falx_set_option(engine.ctx, _lib.OPT_PIPELINE, 1)
+    assert np.array_equal(got[0], want[0])
+    assert got[1] == want[1]
+    assert np.array_equal(got[4], want[4]) and np.array_equal(got[5], want[5]) and got[6] == want[6]
+    rows = got[1]
+    words = (rows + 63) // 64
+    for k, (_, t) in enumerate(cols):
+        (v, valid, sd), (w, wvalid, wsd) = got[2][k], want[2][k]
+        assert np.array_equal(valid[:words], wvalid[:words]), k
+        if t == fx.STR:
+            assert got[3][k] == want[3][k]
+            assert np.array_equal(v[: rows + 1], w[: rows + 1]) and bytes(sd[: got[3][k]]) == bytes(wsd[: got[3][k]])
+        else:
+            assert np.array_equal(v[:rows].view(np.uint8), w[:rows].view(np.uint8)), k
+    # and the oracle's tape
+    s, e = oracle.parse_tape(doc, dialect)
+    assert np.array_equal(got[4], s) and np.array_equal(got[5], e)
