@@ -58,14 +58,14 @@ struct ColParams {
     uint64_t wait_ns;  // look-back wait limit
     DevHeader *hdr;
     // Launches over consecutive chunks of one input (pipelined host-buffer
-    // calls): the tape counts through this chunk come from seed_hi[1..2]
-    // (written by the chunk's index pass) instead of the header; the launch
+    // calls): the tape counts through this chunk come from seed_hi (the
+    // header after the chunk's index pass) instead of the header; the launch
     // takes the record blocks that end before the chunk's last terminator
     // (all the rest when `last`), from its own ticket, and its last block
     // writes the rows and arena bytes through it to chunk_out[0..4]
     // (chunk_out[5] = 1 once written).
-    const uint32_t *seed_lo;  // the previous chunk's seed record, NULL for the first chunk
-    const uint32_t *seed_hi;
+    const SeedRec *seed_lo;  // the previous chunk's seed record, NULL for the first chunk
+    const SeedRec *seed_hi;
     uint32_t *ticket;
     unsigned long long *chunk_out;
     uint32_t last;
@@ -882,8 +882,8 @@ __global__ void __launch_bounds__(kThreads, 3) columns_kernel(const __grid_const
     const int tid = threadIdx.x;
     TapeCounts tc;
     if (p.seed_hi) {
-        tc.n_ends = p.seed_hi[2];
-        tc.n_seps = (uint64_t)p.seed_hi[1] - p.seed_hi[2];
+        tc.n_ends = p.seed_hi->n_terms;
+        tc.n_seps = p.seed_hi->n_struct - p.seed_hi->n_terms;
     } else {
         tc.n_ends = *(volatile const unsigned long long *)&p.hdr->n_terms;
         tc.n_seps = *(volatile const unsigned long long *)&p.hdr->n_struct - tc.n_ends;
@@ -892,7 +892,7 @@ __global__ void __launch_bounds__(kThreads, 3) columns_kernel(const __grid_const
     tc.n_blocks = (uint32_t)((tc.n_recs + kRecBlock - 1) / kRecBlock);
     tc.blk_lo = 0;
     if (p.seed_hi && !p.last) tc.n_blocks = (uint32_t)(tc.n_ends / kRecBlock);  // blocks whose records all end here
-    if (p.seed_lo) tc.blk_lo = p.seed_lo[2] / kRecBlock;  // the previous chunk's launch took the blocks before
+    if (p.seed_lo) tc.blk_lo = (uint32_t)(p.seed_lo->n_terms / kRecBlock);  // the previous chunk's launch took the blocks before
     if (tc.n_seps > p.seps_cap || tc.n_ends > p.ends_cap) {
         if (tid == 0 && blockIdx.x == 0) atomicOr(&p.hdr->error, ERR_TAPE);
         return;

@@ -578,8 +578,10 @@ int setup_spec_kernel(falx_ctx *c) {
 
 template <int D>
 int setup_pass_kernel(falx_ctx *c) {
-    const void *fn = (const void *)index_pass_kernel<D>;
+    const void *fn = (const void *)index_pass_kernel<D, false>;
     FALX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(IxSmem)));
+    FALX_CUDA(cudaFuncSetAttribute((const void *)index_pass_kernel<D, true>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(IxSmem)));
     int nb = 0;
     FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kIxThreads, sizeof(IxSmem)));
     c->blocks_per_sm_pass[D] = nb > 0 ? nb : 1;
@@ -659,8 +661,10 @@ int launch_scan(falx_ctx *c, int dialect, bool rows, const uint8_t *data, uint64
             err = cudaLaunchCooperativeKernel((const void *)index_kernel<D, true>, dim3((unsigned)grid), \
                                               dim3(kThreads), args_, sizeof(SmemIx), c->stream);         \
         else if (pass)                                                                            \
-            err = cudaLaunchCooperativeKernel((const void *)index_pass_kernel<D>, dim3((unsigned)grid), \
-                                              dim3(kIxThreads), args_, sizeof(IxSmem), c->stream);       \
+            err = cudaLaunchCooperativeKernel(P.seed_in ? (const void *)index_pass_kernel<D, true>        \
+                                                        : (const void *)index_pass_kernel<D, false>,     \
+                                              dim3((unsigned)grid), dim3(kIxThreads), args_,             \
+                                              sizeof(IxSmem), c->stream);                                \
         else                                                                                      \
             err = cudaLaunchCooperativeKernel((const void *)index_kernel<D>, dim3((unsigned)grid),     \
                                               dim3(kThreads), args_, sizeof(SmemIx), c->stream);         \
@@ -886,11 +890,13 @@ struct HostPipe {
     const falx_schema *schema;
 };
 
-constexpr int kPipeChunks = 8;
+constexpr int kPipeChunks = 16;                 // at most
+constexpr uint64_t kPipeChunkBytes = 128ull << 20;  // about this much input per chunk (1 GiB: 8 chunks,
+                                                    // measured 8.9 ms against 9.1 ms for 16)
 constexpr int kPipeRetry = 1;  // the tape outgrew its scratch: run the whole-input path instead
 
-// Rows of a host-buffer call as a pipeline over kPipeChunks input chunks
-// (whole tiles each): copy stream H2D chunk k; compute stream: index pass
+// Rows of a host-buffer call as a pipeline over input chunks of whole tiles
+// (about kPipeChunkBytes each, 2 to kPipeChunks of them): copy stream H2D chunk k; compute stream: index pass
 // over chunk k seeded from chunk k - 1's exit state and counts (device
 // records, no host round trip), columns kernel over the record blocks that
 // end inside chunks 0..k; out stream: chunk k's index, tape, column values,
@@ -908,20 +914,24 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
     if (!c->in_free) FALX_CUDA(cudaEventCreateWithFlags(&c->in_free, cudaEventDisableTiming));
     for (int k = 0; k < 2 * kPipeChunks; k++)
         if (!c->pipe_ev[k]) FALX_CUDA(cudaEventCreateWithFlags(&c->pipe_ev[k], cudaEventDisableTiming));
-    // device: seed records (kPipeChunks + 1) x 3 u32 | tickets | per-chunk totals 6 u64 each
-    constexpr size_t kSeedB = (kPipeChunks + 1) * 3 * 4, kTickB = kPipeChunks * 4, kOutB = kPipeChunks * 6 * 8;
+    // device: seed records (kPipeChunks + 1) | tickets | per-chunk totals 6 u64 each
+    static_assert(offsetof(DevHeader, error) == 8 && offsetof(DevHeader, exit_state) == 12 &&
+                      offsetof(DevHeader, n_struct) == 16 && offsetof(DevHeader, n_terms) == 24,
+                  "a seed record is bytes [8, 32) of the header");
+    constexpr size_t kSeedB = (kPipeChunks + 1) * sizeof(SeedRec), kTickOff = 416, kOutB = kPipeChunks * 6 * 8;
     constexpr size_t kPipeB = 512 + kOutB;
-    static_assert(kSeedB + kTickB <= 512, "pipeline records");
+    static_assert(kSeedB <= kTickOff && kTickOff + kPipeChunks * 4 <= 512, "pipeline records");
     if (!c->pipe_dev) FALX_CUDA(cudaMalloc(&c->pipe_dev, kPipeB));
     if (!c->pipe_host) FALX_CUDA(cudaHostAlloc(&c->pipe_host, kPipeB, cudaHostAllocDefault));
-    uint32_t *seeds = c->pipe_dev;
-    uint32_t *tickets = c->pipe_dev + (kPipeChunks + 1) * 3;
+    SeedRec *seeds = reinterpret_cast<SeedRec *>(c->pipe_dev);
+    uint32_t *tickets = reinterpret_cast<uint32_t *>(reinterpret_cast<uint8_t *>(c->pipe_dev) + kTickOff);
     unsigned long long *chunk_out = reinterpret_cast<unsigned long long *>(reinterpret_cast<uint8_t *>(c->pipe_dev) + 512);
-    const uint32_t *h_seeds = reinterpret_cast<const uint32_t *>(c->pipe_host);
+    const SeedRec *h_seeds = reinterpret_cast<const SeedRec *>(c->pipe_host);
     const unsigned long long *h_out = c->pipe_host + 64;
     // chunks of whole tiles (the device input is 256-byte aligned)
     const uint64_t tiles = (len + kTile - 1) / kTile;
-    const uint64_t ct = (tiles + kPipeChunks - 1) / kPipeChunks;
+    const uint64_t want_k = std::min<uint64_t>(kPipeChunks, std::max<uint64_t>(2, len / kPipeChunkBytes));
+    const uint64_t ct = (tiles + want_k - 1) / want_k;
     const int nk = (int)((tiles + ct - 1) / ct);
     auto off = [&](int k) { return std::min(len, (uint64_t)k * ct * kTile); };
     // tape scratch sized from the input; a tape that outgrows it sends the
@@ -960,10 +970,12 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
         Pk.entry0 = 0;
         Pk.pos_base = off(k);
         Pk.sep_base = 0;
-        Pk.seed_in = k > 0 ? seeds + 3 * k : nullptr;
-        Pk.seed_out = seeds + 3 * (k + 1);
+        Pk.seed_in = k > 0 ? seeds + k : nullptr;
         rc = launch_scan(c, dialect, false, dev_in + off(k), off(k + 1) - off(k), Pk, false, true);
         if (rc) return rc;
+        // where chunk k ends: its exit state and the totals through it
+        FALX_CUDA(cudaMemcpyAsync(seeds + k + 1, reinterpret_cast<const uint8_t *>(c->hdr) + 8, sizeof(SeedRec),
+                                  cudaMemcpyDeviceToDevice, c->stream));
         ColParams cp;
         memset(&cp, 0, sizeof cp);
         cp.data = dev_in;
@@ -978,8 +990,8 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
         cp.status = static_cast<BlkStatus *>(c->rec_sums);
         cp.epoch = col_epoch;
         cp.wait_ns = kWaitNs;
-        cp.seed_lo = k > 0 ? seeds + 3 * k : nullptr;
-        cp.seed_hi = seeds + 3 * (k + 1);
+        cp.seed_lo = k > 0 ? seeds + k : nullptr;
+        cp.seed_hi = seeds + k + 1;
         cp.ticket = tickets + k;
         cp.chunk_out = chunk_out + 6 * k;
         cp.last = k == nk - 1;
@@ -1012,7 +1024,7 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
     auto clampu = [](uint64_t v, uint64_t cap) { return v < cap ? v : cap; };
     for (int k = 0; k < nk; k++) {
         FALX_CUDA(cudaEventSynchronize(c->pipe_ev[kPipeChunks + k]));
-        const uint64_t s_k = h_seeds[3 * (k + 1) + 1], t_k = h_seeds[3 * (k + 1) + 2];
+        const uint64_t s_k = h_seeds[k + 1].n_struct, t_k = h_seeds[k + 1].n_terms;
         const bool wrote = h_out[6 * k + 5] != 0;
         const uint64_t rows_k = wrote ? h_out[6 * k] : prow;
         uint64_t arena_k[kMaxStr];

@@ -623,7 +623,9 @@ __device__ __forceinline__ void ix_issue(const Params &p, IxSmem &S, uint32_t t,
 __device__ __forceinline__ bool ix_stopped(IxSmem &S) { return *(volatile uint32_t *)&S.stop != 0; }
 __device__ __forceinline__ void ix_set_stop(IxSmem &S) { *(volatile uint32_t *)&S.stop = 1; }
 
-template <int D>
+// SEED: the launch's entry state and counts come from p.seed_in (chunks of
+// a pipelined call); without it they are p.entry0 and zero.
+template <int D, bool SEED = false>
 __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_constant__ Params p) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     IxSmem &S = *reinterpret_cast<IxSmem *>(smem_raw);
@@ -656,8 +658,9 @@ __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_
     __syncthreads();
     if (warp >= kIxSched) {
         // ---- scheduler warp: the look-backs, in group order
-        const uint32_t e0 = p.seed_in ? p.seed_in[0] : p.entry0;
-        const uint32_t b0s = p.seed_in ? p.seed_in[1] : 0u, b0t = p.seed_in ? p.seed_in[2] : 0u;
+        const uint32_t e0 = SEED ? p.seed_in->exit_state : p.entry0;
+        const uint32_t b0s = SEED ? (uint32_t)p.seed_in->n_struct : 0u;
+        const uint32_t b0t = SEED ? (uint32_t)p.seed_in->n_terms : 0u;
         for (uint32_t j = (uint32_t)(warp - kIxSched); j < own; j += kIxScheds) {
             const uint32_t g = blockIdx.x + j * G;
             const int gs = (int)(j & 1);
@@ -696,11 +699,7 @@ __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_
                 if (g == groups - 1) {
                     p.hdr->n_struct = cs;
                     p.hdr->n_terms = ct;
-                    if (p.seed_out) {
-                        p.seed_out[0] = s;
-                        p.seed_out[1] = cs;
-                        p.seed_out[2] = ct;
-                    }
+                    p.hdr->exit_state = s;
                 }
             }
             __syncwarp();

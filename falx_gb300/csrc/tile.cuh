@@ -41,7 +41,7 @@ struct DevHeader {
     uint32_t ticket;
     uint32_t abort;
     uint32_t error;
-    uint32_t pad;
+    uint32_t exit_state;  // the index pass's exit state at the end of its input
     unsigned long long n_struct, n_terms, n_rows;
     unsigned long long arena[kMaxStr];
     unsigned long long fb_fields, fb_bytes;
@@ -51,6 +51,15 @@ struct DevHeader {
     uint32_t col_ticket;              // record blocks taken by the columns pass
     uint32_t pad2;
 };
+
+// Where a launch over one chunk of a pipelined call ends: bytes [8, 32) of
+// the header after the chunk's index pass, copied aside for the next chunk.
+struct SeedRec {
+    uint32_t error;
+    uint32_t exit_state;
+    unsigned long long n_struct, n_terms;  // through the chunk
+};
+static_assert(sizeof(SeedRec) == 24, "seed record");
 
 // ERR_TAPE: the tape outgrew the buffers it was written to (the host sizes
 // them exactly and runs again)
@@ -91,11 +100,8 @@ struct Params {
     uint32_t chunk_tiles;
     // Index-pass launches over consecutive chunks of one input (pipelined
     // host-buffer calls): the entry state and the structurals / terminators
-    // before the chunk are read from seed_in[0..2] (written by the previous
-    // chunk's launch), and the chunk's last group writes its exit state and
-    // the totals through the chunk to seed_out[0..2].
-    const uint32_t *seed_in;
-    uint32_t *seed_out;
+    // before the chunk, from the previous chunk's seed record.
+    const SeedRec *seed_in;
     RowSpec rows;
 };
 
