@@ -23,6 +23,7 @@ call). Errors raise FalxError where the reference panics or grows a Vec.
 """
 
 import ctypes
+import warnings
 from ctypes import byref, c_uint64, c_void_p
 
 import numpy as np
@@ -104,7 +105,10 @@ class Engine:
                 raise ValueError("data tensor must be contiguous uint8")
             return t
         arr = np.frombuffer(memoryview(data), dtype=np.uint8) if not isinstance(data, np.ndarray) else data
-        return torch.from_numpy(np.ascontiguousarray(arr, dtype=np.uint8)).to("cuda:%d" % self.device)
+        with warnings.catch_warnings():
+            # a read-only view of bytes: torch only reads it, for the copy to the device
+            warnings.simplefilter("ignore", UserWarning)
+            return torch.from_numpy(np.ascontiguousarray(arr, dtype=np.uint8)).to("cuda:%d" % self.device)
 
     def empty(self, n, dtype):
         return self.torch.empty(max(int(n), 1), dtype=dtype, device="cuda:%d" % self.device)

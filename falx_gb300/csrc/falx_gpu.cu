@@ -890,13 +890,14 @@ struct HostPipe {
     const falx_schema *schema;
 };
 
-constexpr int kPipeChunks = 16;                 // at most
-constexpr uint64_t kPipeChunkBytes = 128ull << 20;  // about this much input per chunk (1 GiB: 8 chunks,
-                                                    // measured 8.9 ms against 9.1 ms for 16)
+constexpr int kPipeChunks = 16;                    // at most
+constexpr uint64_t kPipeFirstBytes = 32ull << 20;   // the first and last chunks
+constexpr uint64_t kPipeChunkBytes = 192ull << 20;  // the middle chunks, about
 constexpr int kPipeRetry = 1;  // the tape outgrew its scratch: run the whole-input path instead
 
 // Rows of a host-buffer call as a pipeline over input chunks of whole tiles
-// (about kPipeChunkBytes each, 2 to kPipeChunks of them): copy stream H2D chunk k; compute stream: index pass
+// (ramping from kPipeFirstBytes up to about kPipeChunkBytes and back down,
+// at most kPipeChunks): copy stream H2D chunk k; compute stream: index pass
 // over chunk k seeded from chunk k - 1's exit state and counts (device
 // records, no host round trip), columns kernel over the record blocks that
 // end inside chunks 0..k; out stream: chunk k's index, tape, column values,
@@ -930,10 +931,30 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
     const unsigned long long *h_out = c->pipe_host + 64;
     // chunks of whole tiles (the device input is 256-byte aligned)
     const uint64_t tiles = (len + kTile - 1) / kTile;
-    const uint64_t want_k = std::min<uint64_t>(kPipeChunks, std::max<uint64_t>(2, len / kPipeChunkBytes));
-    const uint64_t ct = (tiles + want_k - 1) / want_k;
-    const int nk = (int)((tiles + ct - 1) / ct);
-    auto off = [&](int k) { return std::min(len, (uint64_t)k * ct * kTile); };
+    // Chunk sizes ramp up from kPipeFirstBytes (doubling) and back down at
+    // the end, with chunks of about kPipeChunkBytes between: the first
+    // outputs start back early and the last chunk's copies are short, so
+    // little of the transfer time falls outside the full pipeline.
+    uint64_t bounds[kPipeChunks + 1];
+    int nk = 0;
+    {
+        uint64_t ramp[4];
+        int nr = 0;
+        uint64_t sum = 0;
+        for (uint64_t step = kPipeFirstBytes / kTile; nr < 4 && step < kPipeChunkBytes / kTile &&
+                                                      2 * (sum + step) <= tiles;
+             step *= 2)
+            ramp[nr++] = step, sum += step;
+        const uint64_t mid = tiles - 2 * sum;
+        uint64_t nm = mid ? (mid + kPipeChunkBytes / kTile - 1) / (kPipeChunkBytes / kTile) : 0;
+        if (nm > (uint64_t)(kPipeChunks - 2 * nr)) nm = kPipeChunks - 2 * nr;
+        uint64_t t = 0;
+        bounds[0] = 0;
+        for (int i = 0; i < nr; i++) bounds[++nk] = t += ramp[i];
+        for (uint64_t i = 0; i < nm; i++) bounds[++nk] = t += mid / nm + (i < mid % nm ? 1 : 0);
+        for (int i = nr - 1; i >= 0; i--) bounds[++nk] = t += ramp[i];
+    }
+    auto off = [&](int k) { return std::min(len, bounds[k] * kTile); };
     // tape scratch sized from the input; a tape that outgrows it sends the
     // call to the whole-input path
     const uint64_t want_seps = (len / 6 + 1024) * 4, want_ends = (len / 24 + 1024) * 8;
