@@ -37,7 +37,17 @@ struct LineView {
     __device__ __forceinline__ uint8_t at(int64_t i) const { return (i >= s0 && i < s1) ? sm[i - s0] : g[i]; }
 };
 
-__device__ __forceinline__ void j_ws(const LineView &v, int64_t e, int64_t &i) {
+// A line staged whole in shared memory: positions relative to the staged
+// window, 32-bit, no per-byte range test (nearly every line).
+struct SmemView {
+    const uint8_t *sm;
+    __device__ __forceinline__ uint8_t at(int i) const { return sm[i]; }
+};
+
+// The scanner below takes either view: V (LineView or SmemView) and the
+// position type I (int64_t or int).
+template <class V, typename I>
+__device__ __forceinline__ void j_ws(const V &v, I e, I &i) {
     while (i < e) {
         uint8_t c = v.at(i);
         if (c != ' ' && c != '\t' && c != '\r') break;
@@ -45,7 +55,8 @@ __device__ __forceinline__ void j_ws(const LineView &v, int64_t e, int64_t &i) {
     }
 }
 
-__device__ __forceinline__ bool j_string(const LineView &v, int64_t e, int64_t &i) {
+template <class V, typename I>
+__device__ __forceinline__ bool j_string(const V &v, I e, I &i) {
     i++;
     while (i < e) {
         uint8_t c = v.at(i);
@@ -56,7 +67,8 @@ __device__ __forceinline__ bool j_string(const LineView &v, int64_t e, int64_t &
     return false;
 }
 
-__device__ inline bool j_skip_value(const LineView &v, int64_t e, int64_t &i) {
+template <class V, typename I>
+__device__ inline bool j_skip_value(const V &v, I e, I &i) {
     j_ws(v, e, i);
     if (i >= e) return false;
     uint8_t c = v.at(i);
@@ -86,15 +98,16 @@ __device__ inline bool j_skip_value(const LineView &v, int64_t e, int64_t &i) {
 }
 
 // Position *i on the value of member `key` of the object opening at *i.
-__device__ inline bool j_member(const LineView &v, int64_t e, int64_t &i, const char *key, int klen) {
+template <class V, typename I>
+__device__ inline bool j_member(const V &v, I e, I &i, const char *key, int klen) {
     if (i >= e || v.at(i) != '{') return false;
     i++;
     for (;;) {
         j_ws(v, e, i);
         if (i >= e || v.at(i) != '"') return false;
-        int64_t ks = i;
+        const I ks = i;
         if (!j_string(v, e, i)) return false;
-        int64_t ke = i;
+        const I ke = i;
         bool match = ke - ks == klen + 2;
         for (int k = 0; match && k < klen; k++) match = v.at(ks + 1 + k) == (uint8_t)key[k];
         j_ws(v, e, i);
@@ -109,7 +122,32 @@ __device__ inline bool j_member(const LineView &v, int64_t e, int64_t &i, const 
     }
 }
 
-__device__ inline bool j_int(const LineView &v, int64_t e, int64_t i, int64_t &out) {
+// Position *i on the value of member `key` among the members that follow
+// the value ending at *i (a ',' and the next member, ...).
+template <class V, typename I>
+__device__ inline bool j_member_next(const V &v, I e, I &i, const char *key, int klen) {
+    for (;;) {
+        j_ws(v, e, i);
+        if (i >= e || v.at(i) != ',') return false;
+        i++;
+        j_ws(v, e, i);
+        if (i >= e || v.at(i) != '"') return false;
+        const I ks = i;
+        if (!j_string(v, e, i)) return false;
+        const I ke = i;
+        bool match = ke - ks == klen + 2;
+        for (int k = 0; match && k < klen; k++) match = v.at(ks + 1 + k) == (uint8_t)key[k];
+        j_ws(v, e, i);
+        if (i >= e || v.at(i) != ':') return false;
+        i++;
+        j_ws(v, e, i);
+        if (match) return true;
+        if (!j_skip_value(v, e, i)) return false;
+    }
+}
+
+template <class V, typename I>
+__device__ inline bool j_int(const V &v, I e, I i, int64_t &out) {
     bool neg = false;
     if (i < e && v.at(i) == '-') { neg = true; i++; }
     if (i >= e) return false;
@@ -127,7 +165,8 @@ __device__ inline bool j_int(const LineView &v, int64_t e, int64_t i, int64_t &o
     return true;
 }
 
-__device__ inline bool j_dec_e6(const LineView &v, int64_t e, int64_t i, int64_t &out) {
+template <class V, typename I>
+__device__ inline bool j_dec_e6(const V &v, I e, I i, int64_t &out) {
     bool neg = false;
     if (i < e && v.at(i) == '-') { neg = true; i++; }
     uint64_t ip = 0;
@@ -159,6 +198,18 @@ __device__ inline bool j_dec_e6(const LineView &v, int64_t e, int64_t i, int64_t
     uint64_t m = ip * 1000000ull + fr;
     out = neg ? -(int64_t)m : (int64_t)m;
     return true;
+}
+
+// One line [j, e): 1 and its id and score, 0 outside the schema, -1 blank.
+template <class V, typename I>
+__device__ __forceinline__ int nd_line(const V &v, I j, I e, int64_t &id, int64_t &sc) {
+    j_ws(v, e, j);
+    if (j >= e) return -1;
+    I a = j, b = j;
+    if (!j_member(v, e, a, "id", 2) || !j_int(v, e, a, id) || !j_member(v, e, b, "nested", 6) ||
+        !j_member(v, e, b, "score", 5) || !j_dec_e6(v, e, b, sc))
+        return 0;
+    return 1;
 }
 
 constexpr int kNdTile = 16384;  // a tile owns the lines that start inside it
@@ -244,12 +295,17 @@ __global__ void __launch_bounds__(kThreads) ndjson_kernel(const uint8_t *data, u
                 while (e < (int64_t)len && data[e] != '\n') e++;
                 if (e > (int64_t)len) e = (int64_t)len;
             }
-            int64_t j = p;
-            j_ws(v, e, j);
-            if (j >= e) continue;
-            int64_t a = j, b = j, id, sc;
-            if (!j_member(v, e, a, "id", 2) || !j_int(v, e, a, id) || !j_member(v, e, b, "nested", 6) ||
-                !j_member(v, e, b, "score", 5) || !j_dec_e6(v, e, b, sc)) {
+            int64_t id, sc;
+            int st;
+            if (e <= t0 + kNdSpan) {
+                // the whole line is staged
+                const SmemView sv{S.buf + 16};
+                st = nd_line(sv, (int)(p - t0), (int)(e - t0), id, sc);
+            } else {
+                st = nd_line(v, p, e, id, sc);
+            }
+            if (st < 0) continue;  // a blank line
+            if (st == 0) {
                 bad = true;
                 continue;
             }
