@@ -122,30 +122,6 @@ __device__ inline bool j_member(const V &v, I e, I &i, const char *key, int klen
     }
 }
 
-// Position *i on the value of member `key` among the members that follow
-// the value ending at *i (a ',' and the next member, ...).
-template <class V, typename I>
-__device__ inline bool j_member_next(const V &v, I e, I &i, const char *key, int klen) {
-    for (;;) {
-        j_ws(v, e, i);
-        if (i >= e || v.at(i) != ',') return false;
-        i++;
-        j_ws(v, e, i);
-        if (i >= e || v.at(i) != '"') return false;
-        const I ks = i;
-        if (!j_string(v, e, i)) return false;
-        const I ke = i;
-        bool match = ke - ks == klen + 2;
-        for (int k = 0; match && k < klen; k++) match = v.at(ks + 1 + k) == (uint8_t)key[k];
-        j_ws(v, e, i);
-        if (i >= e || v.at(i) != ':') return false;
-        i++;
-        j_ws(v, e, i);
-        if (match) return true;
-        if (!j_skip_value(v, e, i)) return false;
-    }
-}
-
 template <class V, typename I>
 __device__ inline bool j_int(const V &v, I e, I i, int64_t &out) {
     bool neg = false;
