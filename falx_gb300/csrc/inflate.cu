@@ -54,16 +54,23 @@ struct WarpSink {
     }
 };
 
+// Members are taken from an atomic ticket, one per warp at a time
+// (members differ in decode time; a static split left warps idle at the
+// end). `counters`: [0] failed members, [1] the ticket.
 __global__ void __launch_bounds__(kGzThreads) inflate_kernel(const uint8_t *comp, uint64_t comp_len,
                                                               const Block *blocks, uint32_t nblocks, uint8_t *out,
                                                               uint64_t out_cap, int32_t *status,
-                                                              unsigned long long *failed) {
+                                                              unsigned long long *counters) {
     __shared__ Tables T[kGzWarps];
     __shared__ Consts K;
     if (threadIdx.x == 0) make_consts(K);
     __syncthreads();
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t b = blockIdx.x * kGzWarps + warp; b < nblocks; b += gridDim.x * kGzWarps) {
+    for (;;) {
+        uint32_t b = 0;
+        if (lane == 0) b = (uint32_t)atomicAdd(counters + 1, 1ull);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (b >= nblocks) break;
         const Block B = blocks[b];
         int rc;
         if (B.in_off > comp_len || B.in_len > comp_len - B.in_off || B.out_off > out_cap ||
@@ -76,7 +83,7 @@ __global__ void __launch_bounds__(kGzThreads) inflate_kernel(const uint8_t *comp
         }
         if (lane == 0) {
             status[b] = rc;
-            if (rc) atomicAdd(failed, 1ull);
+            if (rc) atomicAdd(counters, 1ull);
         }
         __syncwarp();
     }
@@ -160,7 +167,7 @@ int falx_bgzf_inflate(falx_ctx *c, const uint8_t *comp, uint64_t comp_len, const
     FALX_CUDA(cudaSetDevice(c->device));
     // scratch: the block table, then per-block status and the failure count
     const uint64_t tbytes = n_blocks * sizeof(Block), sbytes = n_blocks * 4;
-    const uint64_t need = ((tbytes + 255) & ~255ull) + ((sbytes + 255) & ~255ull) + 256;
+    const uint64_t need = ((tbytes + 255) & ~255ull) + ((sbytes + 255) & ~255ull) + 256;  // + failures, ticket
     if (need > c->gz_cap) {
         if (c->gz_scratch) cudaFree(c->gz_scratch);
         c->gz_scratch = nullptr;
@@ -174,7 +181,7 @@ int falx_bgzf_inflate(falx_ctx *c, const uint8_t *comp, uint64_t comp_len, const
     unsigned long long *dfailed =
         reinterpret_cast<unsigned long long *>(base + ((tbytes + 255) & ~255ull) + ((sbytes + 255) & ~255ull));
     FALX_CUDA(cudaMemcpyAsync(dblocks, blocks, tbytes, cudaMemcpyHostToDevice, c->stream));
-    FALX_CUDA(cudaMemsetAsync(dfailed, 0, sizeof(unsigned long long), c->stream));
+    FALX_CUDA(cudaMemsetAsync(dfailed, 0, 2 * sizeof(unsigned long long), c->stream));
     if (!c->gz_grid) {
         int nb = 0;
         FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, inflate_kernel, kGzThreads, 0));
