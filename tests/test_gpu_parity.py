@@ -233,6 +233,46 @@ def test_ndjson_generated(engine):
     assert st.total_f64 == want["total_f64"]
 
 
+def ndjson_mixed_doc(rng, size):
+    """Stretches of blank and whitespace lines between tiny records (more
+    lines per 16 KiB tile than the kernel deals out one per thread), tiny
+    records alone, records longer than the 4 KiB staging halo, and
+    generated records."""
+    out = bytearray()
+    stretch = 0
+    while len(out) < size:
+        kind = stretch % 4
+        stretch += 1
+        if kind == 0:
+            for _ in range(3000):
+                k = rng.next() % 4
+                out += [b"\n", b" \n", b"\t \n",
+                        b'{"id":%d,"nested":{"score":%d}}\n' % (rng.next() % 50, rng.next() % 9)][k]
+        elif kind == 1:
+            for _ in range(1500):
+                out += b'{"id":-%d,"nested":{"score":%d.%d}}\n' % (rng.next() % 999, rng.next() % 99, rng.next() % 9)
+        elif kind == 2:
+            for _ in range(6):
+                pad = b"x" * (3000 + rng.next() % 9000)
+                out += b'{"note":"%s","id":%d,"nested":{"ok":true,"score":%d}}\n' % (pad, rng.next() % 7, rng.next() % 5)
+        else:
+            out += gen.generate(gen.NDJSON, 40_000 + rng.next() % 30_000, seed=rng.next() % 1000).tobytes()
+    return bytes(out)
+
+
+@pytest.mark.parametrize("shift", [0, 5])
+def test_ndjson_dense_and_long_lines(engine, shift):
+    doc = ndjson_mixed_doc(Rng(77 + shift), 3 << 20)
+    buf = engine.to_device(np.frombuffer(b" " * shift + doc, dtype=np.uint8))[shift:]
+    st = engine.ndjson_id_score(buf)
+    want = oracle.ndjson_json(doc)
+    assert want is not None
+    assert st.records == want["records"]
+    assert st.sum_id == want["sum_id"]
+    assert st.sum_score_e6 == want["sum_score_e6"]
+    assert st.total_e6 == want["total_e6"]
+
+
 def dense_mixed_doc(rng, dialect, size):
     """Stretches of very short fields (more structurals per 16 KiB tile than
     the row kernel stages) between stretches of ordinary rows."""
