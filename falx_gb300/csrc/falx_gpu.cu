@@ -883,6 +883,20 @@ int rows_two_pass(falx_ctx *c, int dialect, const uint8_t *data, uint64_t len, P
     return FALX_OK;
 }
 
+// Chunk k of a pipelined call is done: its seed record and totals stored to
+// mapped host memory (one warp).
+__global__ void pipe_publish_kernel(const SeedRec *seed, const unsigned long long *out, SeedRec *h_seed,
+                                    unsigned long long *h_out) {
+    const int t = threadIdx.x;
+    if (t == 0) {
+        h_seed->error = seed->error;
+        h_seed->exit_state = seed->exit_state;
+        h_seed->n_struct = seed->n_struct;
+        h_seed->n_terms = seed->n_terms;
+    }
+    if (t < 6) h_out[t] = out[t];
+}
+
 // Host buffers of a pipelined falx_parse_host call.
 struct HostPipe {
     const uint8_t *in;      // the input (host)
@@ -923,12 +937,17 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
     constexpr size_t kPipeB = 512 + kOutB;
     static_assert(kSeedB <= kTickOff && kTickOff + kPipeChunks * 4 <= 512, "pipeline records");
     if (!c->pipe_dev) FALX_CUDA(cudaMalloc(&c->pipe_dev, kPipeB));
-    if (!c->pipe_host) FALX_CUDA(cudaHostAlloc(&c->pipe_host, kPipeB, cudaHostAllocDefault));
+    if (!c->pipe_host) FALX_CUDA(cudaHostAlloc(&c->pipe_host, kPipeB, cudaHostAllocMapped));
     SeedRec *seeds = reinterpret_cast<SeedRec *>(c->pipe_dev);
     uint32_t *tickets = reinterpret_cast<uint32_t *>(reinterpret_cast<uint8_t *>(c->pipe_dev) + kTickOff);
     unsigned long long *chunk_out = reinterpret_cast<unsigned long long *>(reinterpret_cast<uint8_t *>(c->pipe_dev) + 512);
-    const SeedRec *h_seeds = reinterpret_cast<const SeedRec *>(c->pipe_host);
-    const unsigned long long *h_out = c->pipe_host + 64;
+    const volatile SeedRec *h_seeds = reinterpret_cast<const volatile SeedRec *>(c->pipe_host);
+    const volatile unsigned long long *h_out = c->pipe_host + 64;
+    // the same host records as the kernels see them (mapped pinned memory)
+    unsigned long long *host_map = nullptr;
+    FALX_CUDA(cudaHostGetDevicePointer((void **)&host_map, c->pipe_host, 0));
+    SeedRec *host_seeds = reinterpret_cast<SeedRec *>(host_map);
+    unsigned long long *host_out = host_map + 64;
     // chunks of whole tiles (the device input is 256-byte aligned)
     const uint64_t tiles = (len + kTile - 1) / kTile;
     // Chunk sizes ramp up from kPipeFirstBytes (doubling) and back down at
@@ -992,11 +1011,9 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
         Pk.pos_base = off(k);
         Pk.sep_base = 0;
         Pk.seed_in = k > 0 ? seeds + k : nullptr;
+        Pk.seed_out = seeds + k + 1;  // where chunk k ends: its exit state and the totals through it
         rc = launch_scan(c, dialect, false, dev_in + off(k), off(k + 1) - off(k), Pk, false, true);
         if (rc) return rc;
-        // where chunk k ends: its exit state and the totals through it
-        FALX_CUDA(cudaMemcpyAsync(seeds + k + 1, reinterpret_cast<const uint8_t *>(c->hdr) + 8, sizeof(SeedRec),
-                                  cudaMemcpyDeviceToDevice, c->stream));
         ColParams cp;
         memset(&cp, 0, sizeof cp);
         cp.data = dev_in;
@@ -1031,9 +1048,12 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
         default: FALX_COLS(D_LOGFMT); break;
         }
 #undef FALX_COLS
+        // chunk k's seed record and totals to the host by a store kernel (a
+        // copy on this stream would queue behind the out stream's copies
+        // back on the copy engine, and hold up the next chunk's kernels)
+        pipe_publish_kernel<<<1, 32, 0, c->stream>>>(seeds + k + 1, chunk_out + 6 * k, host_seeds + k + 1,
+                                                     host_out + 6 * k);
         FALX_CUDA(cudaGetLastError());
-        FALX_CUDA(cudaMemcpyAsync(c->pipe_host, seeds, kSeedB, cudaMemcpyDeviceToHost, c->stream));
-        FALX_CUDA(cudaMemcpyAsync(c->pipe_host + 64, chunk_out, kOutB, cudaMemcpyDeviceToHost, c->stream));
         FALX_CUDA(cudaEventRecord(c->pipe_ev[kPipeChunks + k], c->stream));
     }
     // copy each chunk's outputs back as soon as its totals are in
@@ -1593,7 +1613,7 @@ int falx_parse_host(falx_ctx *c, const falx_schema *schema, const uint8_t *host_
     const bool rows_call = hc || host_out->field_bytes || host_out->stats;
     // columns over a large input: the pipelined form (copies in and out
     // overlap the parse, rows_pipelined)
-    const bool pipelined = c->pipeline && hc && len >= kChunkedInMin && c->rows_path == 0 &&
+    const bool pipelined = c->pipeline && hc && len >= kChunkedInMin && c->rows_path == 0 && !c->old_index &&
                            schema->dialect != FALX_NDJSON;
     bool chunked = false, copied = pipelined;
     if (!pipelined && len >= kChunkedInMin && rows_call && c->rows_path == 0 && schema->dialect != FALX_NDJSON) {

@@ -700,6 +700,11 @@ __global__ void __launch_bounds__(kIxThreads, 3) index_pass_kernel(const __grid_
                     p.hdr->n_struct = cs;
                     p.hdr->n_terms = ct;
                     p.hdr->exit_state = s;
+                    if (p.seed_out) {
+                        p.seed_out->exit_state = s;
+                        p.seed_out->n_struct = cs;
+                        p.seed_out->n_terms = ct;
+                    }
                 }
             }
             __syncwarp();

@@ -52,8 +52,9 @@ struct DevHeader {
     uint32_t pad2;
 };
 
-// Where a launch over one chunk of a pipelined call ends: bytes [8, 32) of
-// the header after the chunk's index pass, copied aside for the next chunk.
+// Where a launch over one chunk of a pipelined call ends (the exit state and
+// the structurals / terminators through the chunk), written by the chunk's
+// index pass for the next chunk. `error` is not used.
 struct SeedRec {
     uint32_t error;
     uint32_t exit_state;
@@ -102,6 +103,7 @@ struct Params {
     // host-buffer calls): the entry state and the structurals / terminators
     // before the chunk, from the previous chunk's seed record.
     const SeedRec *seed_in;
+    SeedRec *seed_out;  // optional: where the launch ends (exit state, totals), for the next chunk
     RowSpec rows;
 };
 
