@@ -534,6 +534,8 @@ __device__ __forceinline__ uint32_t ix_place(IxSmem &S, int slot, int lane, uint
     return tot;
 }
 
+__device__ __forceinline__ uint32_t cap32(uint64_t cap) { return cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap; }
+
 // Output of a tile (compute threads, after its look-back): the thread's
 // masks under its true entry state, ranks within the warp, then the warp's
 // index and tape entries from a staged list, coalesced.
@@ -564,49 +566,57 @@ __device__ __forceinline__ void ix_output(const Params &p, IxSmem &S, uint32_t t
     const uint32_t woff = S.woff[rs][warp], ce = x - c;
     const uint32_t n = __shfl_sync(0xffffffffu, x, 31) & 0xFFFFu;  // the warp's structurals
     const uint32_t my0 = ce & 0xFFFFu, my1 = my0 + (c & 0xFFFFu);   // my ranks within the warp
-    const uint64_t gs0 = (uint64_t)S.base_s[rs] + (woff & 0xFFFFu);  // structurals before the warp's run
-    uint64_t gt = (uint64_t)S.base_t[rs] + (woff >> 16);              // terminators before the batch
+    // Ordinals and positions in 32 bits: a launch's input is shorter than
+    // 4 GiB, so its counts and positions (base included) fit.
+    const uint32_t gs0 = S.base_s[rs] + (woff & 0xFFFFu);  // structurals before the warp's run
+    uint32_t gt = S.base_t[rs] + (woff >> 16);              // terminators before the batch
     const uint32_t pbase = (uint32_t)(p.pos_base + vs);
+    const uint32_t sbase = (uint32_t)p.sep_base;            // ends keep the low 32 bits of the separator count
+    const uint32_t icap = p.index ? cap32(p.index_cap) : 0u;
+    const uint32_t scap = p.seps ? cap32(p.seps_cap) : 0u;
+    const uint32_t ecap = p.ends ? cap32(p.ends_cap) : 0u;
     const uint32_t lt = (1u << lane) - 1u;
-    const bool tape = p.seps || p.ends;
+    const uint32_t at = (uint32_t)tid * kThreadBytes;
     uint16_t *stage = S.stage[warp];
     // batches of kIxStage ranks: stage (tile offset, bit 15 = terminator) in
     // rank order, then write index and tape entries coalesced
     for (uint32_t lo = 0; lo < n; lo += kIxStage) {
         const uint32_t hi = min(lo + (uint32_t)kIxStage, n);
-        if (my1 > lo && my0 < hi) {
+        if (n <= (uint32_t)kIxStage) {
+            // one batch (the usual case): all of the thread's structurals
+            uint64_t mm = stm;
             uint32_t k = my0;
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                uint32_t mm = (uint32_t)(stm >> (32 * h));
-                const uint32_t tt = (uint32_t)(term >> (32 * h));
-                const uint32_t at = (uint32_t)(tid * kThreadBytes + 32 * h);
-                while (mm && k < hi) {
-                    const uint32_t bpos = __ffs(mm) - 1;
-                    if (k >= lo) stage[k - lo] = (uint16_t)((at + bpos) | (((tt >> bpos) & 1u) << 15));
-                    k++;
-                    mm &= mm - 1;
-                }
+            while (mm) {
+                const uint32_t b = (uint32_t)__ffsll((long long)mm) - 1u;
+                stage[k++] = (uint16_t)((at + b) | ((uint32_t)(term >> b) & 1u) << 15);
+                mm &= mm - 1;
+            }
+        } else if (my1 > lo && my0 < hi) {
+            uint32_t k = my0;
+            uint64_t mm = stm;
+            while (mm && k < hi) {
+                const uint32_t b = (uint32_t)__ffsll((long long)mm) - 1u;
+                if (k >= lo) stage[k - lo] = (uint16_t)((at + b) | ((uint32_t)(term >> b) & 1u) << 15);
+                k++;
+                mm &= mm - 1;
             }
         }
         __syncwarp();
-        for (uint32_t k = lo; k < hi; k += 32) {
-            const uint32_t kk = k + lane;
+        for (uint32_t q = lo; q < hi; q += 32) {
+            const uint32_t kk = q + lane;
             const bool in = kk < hi;
             const uint32_t e = in ? stage[kk - lo] : 0u;
             const bool is_t = in && (e >> 15);
             const uint32_t bt_mask = __ballot_sync(0xffffffffu, is_t);
-            const uint64_t gs = gs0 + kk;                    // structural ordinal
-            const uint64_t gtt = gt + __popc(bt_mask & lt);  // terminators before it
+            const uint32_t gs = gs0 + kk;                    // structural ordinal
+            const uint32_t gtt = gt + __popc(bt_mask & lt);  // terminators before it
+            const uint32_t gsep = gs - gtt;                  // separators before it
             const uint32_t pos = pbase + (e & 0x7FFFu);
-            if (in && p.index && gs < p.index_cap) p.index[gs] = pos;
-            if (in && tape) {
-                const uint64_t gsep = gs - gtt;  // separators before it
-                if (is_t) {
-                    if (p.ends && gtt < p.ends_cap) p.ends[gtt] = ((p.sep_base + gsep) << 32) | pos;
-                } else if (p.seps && gsep < p.seps_cap) {
-                    p.seps[gsep] = pos;
-                }
+            if (in && gs < icap) p.index[gs] = pos;
+            if (is_t) {
+                if (gtt < ecap) p.ends[gtt] = ((uint64_t)(sbase + gsep) << 32) | pos;
+            } else if (in && gsep < scap) {
+                p.seps[gsep] = pos;
             }
             gt += __popc(bt_mask);
         }
