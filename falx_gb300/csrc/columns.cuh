@@ -164,10 +164,11 @@ __device__ __forceinline__ uint64_t lds_u64(const uint8_t *base, uint32_t o) {
     return (uint64_t)__funnelshift_r(a, b, sh) | ((uint64_t)__funnelshift_r(b, c, sh) << 32);
 }
 
-// 1-8 plain digits at shared offset o (swar.cuh).
+// 1-10 plain digits at shared offset o (swar.cuh).
 __device__ __forceinline__ bool swar_u32(const uint8_t *sd, uint32_t o, uint32_t n, uint32_t &v) {
-    if (n - 1u > 7u) return false;
-    return swar::u32_word(lds_u64(sd, o), n, v);
+    if (n - 1u <= 7u) return swar::u32_word(lds_u64(sd, o), n, v);
+    if (n - 9u <= 1u) return swar::u32_word10(lds_u32(sd, o), lds_u64(sd, o + n - 8u), n, v);
+    return false;
 }
 
 // [+-]?d{1,3}.d{6} at shared offset o (swar.cuh): mantissa m, sign and the

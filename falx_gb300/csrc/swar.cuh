@@ -4,7 +4,8 @@
 // from shared memory; the CPU tests feed them words built from byte
 // strings and compare with str::parse semantics.
 //
-//   u32:     1-8 plain digits (str::parse::<u32> of such a cell).
+//   u32:     1-10 plain digits (str::parse::<u32> of such a cell; a value
+//            above u32::MAX is left to the general decoder).
 //   fixed6:  [+-]?d{1,3}.d{6}: the mantissa m (integer and fraction digits)
 //            and the f64 bits of m / 1e6, correctly rounded
 //            (csv_geo.rs:1414-1475 divides in IEEE arithmetic; Eisel-Lemire
@@ -49,6 +50,19 @@ FALX_HD bool u32_word(uint64_t x, uint32_t n, uint32_t &v) {
     x <<= sh;  // the n bytes at the top, zeros below
     if (!digits_ok(x, ~0ull << sh)) return false;
     v = eight_digits(x);
+    return true;
+}
+
+// n in [9, 10]: h = the 4 bytes from the cell's start (its n - 8 leading
+// digits first), t = the 8 bytes that end the cell (its last 8 digits).
+// Values above u32::MAX are rejected (the general decoder reports them).
+FALX_HD bool u32_word10(uint32_t h, uint64_t t, uint32_t n, uint32_t &v) {
+    const uint32_t hs = 8u * (12u - n);  // the n - 8 leading digits at the top of h
+    h <<= hs;
+    if (!digits_ok(t, ~0ull) || !digits_ok(h, (uint64_t)(0xFFFFFFFFu << hs))) return false;
+    const uint64_t x = (uint64_t)four_digits(h) * 100000000ull + eight_digits(t);
+    if (x > 0xFFFFFFFFull) return false;
+    v = (uint32_t)x;
     return true;
 }
 

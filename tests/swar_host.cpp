@@ -16,8 +16,9 @@ static uint32_t le32(const uint8_t *b) { return (uint32_t)b[0] | (uint32_t)b[1] 
 // `buf` holds the cell at offset 0 followed by at least 8 bytes of padding
 // (whatever follows a cell in the staged window).
 extern "C" int swar_u32_cell(const uint8_t *buf, uint32_t n, uint32_t *v) {
-    if (n - 1u > 7u) return 0;
-    return falx::swar::u32_word(le64(buf), n, *v) ? 1 : 0;
+    if (n - 1u <= 7u) return falx::swar::u32_word(le64(buf), n, *v) ? 1 : 0;
+    if (n - 9u <= 1u) return falx::swar::u32_word10(le32(buf), le64(buf + n - 8), n, *v) ? 1 : 0;
+    return 0;
 }
 
 extern "C" int swar_fixed6_cell(const uint8_t *buf, uint32_t n, uint64_t *bits, uint32_t *m, int *neg) {

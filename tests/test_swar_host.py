@@ -13,7 +13,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-U32_RE = re.compile(rb"[0-9]{1,8}")
+U32_RE = re.compile(rb"[0-9]{1,10}")
 FIXED6_RE = re.compile(rb"[+-]?[0-9]{1,3}\.[0-9]{6}")
 
 
@@ -34,6 +34,8 @@ def cells(rng):
              b"\x80", b"\xba1", b"1\xff", b"0.000000", b"-0.000000", b"+0.000001", b"1.500000", b"-172.432059",
              b"999.999999", b"1000.000000", b"1.5", b"12.3456789", b".123456", b"-.123456", b"1.23456a",
              b"1a.123456", b"+-1.000000", b"1.1234567", b"12.123456", b"123.12345", b"89.999999", b"1:.123456",
+             b"4294967295", b"4294967296", b"9999999999", b"0000000000", b"0004294967", b"2147483648", b"a234567890",
+             b"123456789a", b"12345678901", b"1234\xba67890", b"\xba23456789", b"12345678\xba",
              b"1/.123456", b"\xba.123456", b"1.12345\xba", b"1,000000", b"", b"12.12345."]
     out = list(fixed)
     alphabet = b"0123456789.+-a/:\xba\x80 "
@@ -43,7 +45,7 @@ def cells(rng):
             s = (rng.choice([b"", b"-", b"+"]) + bytes(rng.choice(b"0123456789") for _ in range(rng.randint(1, 3)))
                  + b"." + bytes(rng.choice(b"0123456789") for _ in range(6)))
         elif kind < 0.7:
-            s = bytes(rng.choice(b"0123456789") for _ in range(rng.randint(1, 9)))
+            s = bytes(rng.choice(b"0123456789") for _ in range(rng.randint(1, 11)))
         else:
             s = bytes(rng.choice(alphabet) for _ in range(rng.randint(0, 11)))
         if rng.random() < 0.1 and s:  # one corrupted byte
@@ -61,7 +63,7 @@ def test_u32_and_fixed6_match_str_parse(lib):
     for s in cells(rng):
         buf = s + bytes(rng.randrange(256) for _ in range(8))  # whatever follows the cell
         ok = lib.swar_u32_cell(buf, len(s), ctypes.byref(v))
-        assert ok == bool(U32_RE.fullmatch(s)), s
+        assert ok == bool(U32_RE.fullmatch(s) and int(s) <= 0xFFFFFFFF), s
         if ok:
             accepted[0] += 1
             assert v.value == int(s), s
