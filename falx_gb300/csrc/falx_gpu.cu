@@ -1103,9 +1103,12 @@ int rows_pipelined(falx_ctx *c, int dialect, const uint8_t *dev_in, uint64_t len
                     const uint64_t a = clampu(prow, rcap), b = clampu(rows_k, rcap);
                     if (b > a && (rc = back(hv + es * a, dv + es * a, (b - a) * es))) return rc;
                 }
-                if (wk > pw && (rc = back(hc->cols[j].valid + pw, rs.valid[j] + pw, (wk - pw) * 8))) return rc;
+                // validity words every fourth chunk (small copies cost the
+                // copy engine about as much as large ones)
+                if ((k & 3) == 3 && wk > pw && (rc = back(hc->cols[j].valid + pw, rs.valid[j] + pw, (wk - pw) * 8)))
+                    return rc;
             }
-            pw = wk > pw ? wk : pw;
+            if ((k & 3) == 3) pw = wk > pw ? wk : pw;
             if (rows_k) poff = rows_k + 1;
         }
         ps = s_k;
