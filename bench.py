@@ -378,7 +378,7 @@ def bench_gpu(args):
     e2e = {"value": round(n / GIB / e2e_s, 4), "unit": "GiB/s", "h2d_bytes_per_step": n, "d2h_bytes_per_step": d2h,
            "ms_per_step": round(e2e_s * 1e3, 3), "ms_min_max": [round(min(e2e_t) * 1e3, 3), round(max(e2e_t) * 1e3, 3)],
            "calls": len(e2e_t),
-           "form": ("pipelined: input chunks of 32, 64, 128 MiB, then about 192 MiB, then 128, 64, 32 MiB, each "
+           "form": ("pipelined: input chunks of 16, 32, 64 MiB, then about 96 MiB, then 64, 32, 16 MiB, each "
                     "copied in, parsed and copied back while the others move"),
            "whole_input": {"value": round(n / GIB / float(np.median(whole_t)), 4), "unit": "GiB/s",
                            "ms_per_step": round(float(np.median(whole_t)) * 1e3, 3)}}

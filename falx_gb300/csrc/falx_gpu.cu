@@ -905,8 +905,8 @@ struct HostPipe {
 };
 
 constexpr int kPipeChunks = 16;                    // at most
-constexpr uint64_t kPipeFirstBytes = 32ull << 20;   // the first and last chunks
-constexpr uint64_t kPipeChunkBytes = 192ull << 20;  // the middle chunks, about
+constexpr uint64_t kPipeFirstBytes = 16ull << 20;  // the first and last chunks
+constexpr uint64_t kPipeChunkBytes = 96ull << 20;  // the middle chunks, about
 constexpr int kPipeRetry = 1;  // the tape outgrew its scratch: run the whole-input path instead
 
 // Rows of a host-buffer call as a pipeline over input chunks of whole tiles

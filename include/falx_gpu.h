@@ -73,7 +73,7 @@ void falx_destroy(falx_ctx *ctx);
 #define FALX_OPT_CTAS_PER_SM 2
 #define FALX_OPT_TIMING 3 /* 1: time each launch of the rows path with CUDA events */
 /* FALX_OPT_PIPELINE (default 1): falx_parse_host with columns over 64 MiB or
- * more runs as a pipeline of input chunks (32 MiB first and last, about 192
+ * more runs as a pipeline of input chunks (16 MiB first and last, about 96
  * MiB in the middle):
  * each chunk is copied in,
  * indexed and its records decoded while later chunks are still being copied
