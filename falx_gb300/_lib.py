@@ -121,6 +121,8 @@ SIGNATURES = {
     "falx_bgzf_scan": (c_int, [c_void_p, c_uint64, c_void_p, c_uint64, POINTER(c_uint64), POINTER(c_uint64)]),
     "falx_bgzf_inflate": (c_int, [c_void_p, c_void_p, c_uint64, c_void_p, c_uint64, c_void_p, c_uint64, c_void_p,
                                   POINTER(c_uint64)]),
+    "falx_parse_gz_host": (c_int, [c_void_p, POINTER(falx_schema), c_void_p, c_uint64, c_void_p, c_uint64,
+                                   POINTER(falx_outputs)]),
     "falx_model_param_count": (c_uint64, []),
     "falx_model_create": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
     "falx_model_destroy": (None, [c_void_p]),

@@ -90,9 +90,20 @@ struct falx_ctx {
     void *gz_scratch = nullptr;
     uint64_t gz_cap = 0;
     int gz_grid = 0;
+    uint8_t *gz_comp = nullptr;     // falx_parse_gz_host: the compressed stream in device memory
+    uint64_t gz_comp_cap = 0;
+    unsigned long long *gz_host = nullptr;  // pinned: members that failed to inflate
     // per-launch timing of the last rows call (FALX_OPT_TIMING)
     int timing = 0;
     cudaEvent_t ev[5] = {};
     float last_ms[4] = {};
     int last_n = 0;
 };
+
+namespace falx {
+// Inflate every member of a bgzf stream into `out` on the context's stream
+// without waiting (inflate.cu). *counters (device): [0] members that
+// failed, [1] the member ticket; *status (device): per member.
+int gz_launch(falx_ctx *c, const uint8_t *comp, uint64_t comp_len, const falx_gz_block *blocks, uint64_t n_blocks,
+              uint8_t *out, uint64_t out_cap, unsigned long long **counters, int32_t **status);
+}  // namespace falx

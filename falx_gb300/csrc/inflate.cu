@@ -108,6 +108,45 @@ uint32_t le32(const uint8_t *p) { return (uint32_t)p[0] | ((uint32_t)p[1] << 8) 
 
 using namespace falx::gz;
 
+namespace falx {
+int gz_launch(falx_ctx *c, const uint8_t *comp, uint64_t comp_len, const falx_gz_block *blocks, uint64_t n_blocks,
+              uint8_t *out, uint64_t out_cap, unsigned long long **counters, int32_t **status) {
+    static_assert(sizeof(falx_gz_block) == sizeof(Block), "block layout");
+    // scratch: the block table, then per-block status and the counters
+    const uint64_t tbytes = n_blocks * sizeof(Block), sbytes = n_blocks * 4;
+    const uint64_t need = ((tbytes + 255) & ~255ull) + ((sbytes + 255) & ~255ull) + 256;  // + counters
+    if (need > c->gz_cap) {
+        // earlier launches may still read the old scratch
+        FALX_CUDA(cudaStreamSynchronize(c->stream));
+        if (c->gz_scratch) cudaFree(c->gz_scratch);
+        c->gz_scratch = nullptr;
+        c->gz_cap = 0;
+        FALX_CUDA(cudaMalloc(&c->gz_scratch, need));
+        c->gz_cap = need;
+    }
+    uint8_t *base = static_cast<uint8_t *>(c->gz_scratch);
+    Block *dblocks = reinterpret_cast<Block *>(base);
+    int32_t *dstatus = reinterpret_cast<int32_t *>(base + ((tbytes + 255) & ~255ull));
+    unsigned long long *dcounters =
+        reinterpret_cast<unsigned long long *>(base + ((tbytes + 255) & ~255ull) + ((sbytes + 255) & ~255ull));
+    FALX_CUDA(cudaMemcpyAsync(dblocks, blocks, tbytes, cudaMemcpyHostToDevice, c->stream));
+    FALX_CUDA(cudaMemsetAsync(dcounters, 0, 2 * sizeof(unsigned long long), c->stream));
+    if (!c->gz_grid) {
+        int nb = 0;
+        FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, inflate_kernel, kGzThreads, 0));
+        c->gz_grid = std::max(1, nb) * c->sm_count;
+    }
+    const uint64_t want = (n_blocks + kGzWarps - 1) / kGzWarps;
+    const unsigned grid = (unsigned)std::min<uint64_t>(want, (uint64_t)c->gz_grid);
+    inflate_kernel<<<grid, kGzThreads, 0, c->stream>>>(comp, comp_len, dblocks, (uint32_t)n_blocks, out, out_cap,
+                                                       dstatus, dcounters);
+    FALX_CUDA(cudaGetLastError());
+    *counters = dcounters;
+    *status = dstatus;
+    return FALX_OK;
+}
+}  // namespace falx
+
 extern "C" {
 
 // Walk the gzip members of a bgzf stream (bgzf.rs:42-108): magic 1f 8b,
@@ -159,42 +198,19 @@ int falx_bgzf_scan(const uint8_t *comp, uint64_t len, falx_gz_block *blocks, uin
 int falx_bgzf_inflate(falx_ctx *c, const uint8_t *comp, uint64_t comp_len, const falx_gz_block *blocks,
                       uint64_t n_blocks, uint8_t *out, uint64_t out_cap, int32_t *block_status,
                       uint64_t *n_failed) {
-    static_assert(sizeof(falx_gz_block) == sizeof(Block), "block layout");
     if (!c || (comp_len && !comp) || (n_blocks && !blocks) || (out_cap && !out) || n_blocks > 0xFFFFFFFFull)
         return FALX_ERR_INVALID;
     if (n_failed) *n_failed = 0;
     if (n_blocks == 0) return FALX_OK;
     FALX_CUDA(cudaSetDevice(c->device));
-    // scratch: the block table, then per-block status and the failure count
-    const uint64_t tbytes = n_blocks * sizeof(Block), sbytes = n_blocks * 4;
-    const uint64_t need = ((tbytes + 255) & ~255ull) + ((sbytes + 255) & ~255ull) + 256;  // + failures, ticket
-    if (need > c->gz_cap) {
-        if (c->gz_scratch) cudaFree(c->gz_scratch);
-        c->gz_scratch = nullptr;
-        c->gz_cap = 0;
-        FALX_CUDA(cudaMalloc(&c->gz_scratch, need));
-        c->gz_cap = need;
-    }
-    uint8_t *base = static_cast<uint8_t *>(c->gz_scratch);
-    Block *dblocks = reinterpret_cast<Block *>(base);
-    int32_t *dstatus = reinterpret_cast<int32_t *>(base + ((tbytes + 255) & ~255ull));
-    unsigned long long *dfailed =
-        reinterpret_cast<unsigned long long *>(base + ((tbytes + 255) & ~255ull) + ((sbytes + 255) & ~255ull));
-    FALX_CUDA(cudaMemcpyAsync(dblocks, blocks, tbytes, cudaMemcpyHostToDevice, c->stream));
-    FALX_CUDA(cudaMemsetAsync(dfailed, 0, 2 * sizeof(unsigned long long), c->stream));
-    if (!c->gz_grid) {
-        int nb = 0;
-        FALX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, inflate_kernel, kGzThreads, 0));
-        c->gz_grid = std::max(1, nb) * c->sm_count;
-    }
-    const uint64_t want = (n_blocks + kGzWarps - 1) / kGzWarps;
-    const unsigned grid = (unsigned)std::min<uint64_t>(want, (uint64_t)c->gz_grid);
-    inflate_kernel<<<grid, kGzThreads, 0, c->stream>>>(comp, comp_len, dblocks, (uint32_t)n_blocks, out, out_cap,
-                                                       dstatus, dfailed);
-    FALX_CUDA(cudaGetLastError());
+    unsigned long long *dcounters = nullptr;
+    int32_t *dstatus = nullptr;
+    const int rc = falx::gz_launch(c, comp, comp_len, blocks, n_blocks, out, out_cap, &dcounters, &dstatus);
+    if (rc) return rc;
     unsigned long long failed = 0;
-    FALX_CUDA(cudaMemcpyAsync(&failed, dfailed, sizeof failed, cudaMemcpyDeviceToHost, c->stream));
-    if (block_status) FALX_CUDA(cudaMemcpyAsync(block_status, dstatus, sbytes, cudaMemcpyDeviceToHost, c->stream));
+    FALX_CUDA(cudaMemcpyAsync(&failed, dcounters, sizeof failed, cudaMemcpyDeviceToHost, c->stream));
+    if (block_status)
+        FALX_CUDA(cudaMemcpyAsync(block_status, dstatus, n_blocks * 4, cudaMemcpyDeviceToHost, c->stream));
     FALX_CUDA(cudaStreamSynchronize(c->stream));
     if (n_failed) *n_failed = failed;
     return failed ? FALX_ERR_FORMAT : FALX_OK;

@@ -104,6 +104,9 @@ struct Params {
     // before the chunk, from the previous chunk's seed record.
     const SeedRec *seed_in;
     SeedRec *seed_out;  // optional: where the launch ends (exit state, totals), for the next chunk
+    // seeded launches over a chunk of input already in device memory: the
+    // byte before the chunk is read there (prev_byte is then unused)
+    const uint8_t *prev_ptr;
     RowSpec rows;
 };
 
@@ -450,7 +453,9 @@ __device__ void lookback_cta(const Params &p, LookbackSmem &L, uint32_t tile, ui
 }
 
 // The byte before position 0 of a launch: -1 at the start of a file.
-__device__ __forceinline__ int prev_of(const Params &p) { return p.seeded ? (int)p.prev_byte : -1; }
+__device__ __forceinline__ int prev_of(const Params &p) {
+    return p.seeded ? (p.prev_ptr ? (int)*p.prev_ptr : (int)p.prev_byte) : -1;
+}
 // Position 0 starts a line: at a file start, or after a '\n'.
 __device__ __forceinline__ bool starts_line(int prev) { return prev < 0 || prev == '\n'; }
 

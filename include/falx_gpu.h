@@ -425,6 +425,17 @@ int falx_bgzf_scan(const uint8_t *comp, uint64_t len, falx_gz_block *blocks, uin
  * Synchronous on the context's stream. */
 int falx_bgzf_inflate(falx_ctx *ctx, const uint8_t *comp, uint64_t comp_len, const falx_gz_block *blocks,
                       uint64_t n_blocks, uint8_t *out, uint64_t out_cap, int32_t *block_status, uint64_t *n_failed);
+/* bgzf.rs:538 parse_gz_par with host buffers: falx_parse_host over the text
+ * of the bgzf stream `comp` (host memory; pinned for the copy to overlap),
+ * whose blocks (host, from falx_bgzf_scan: texts end to end from 0) are
+ * inflated on the GPU into device memory, never crossing the host link.
+ * The parse and the copies back are those of falx_parse_host (pipelined for
+ * columns over 64 MiB: the outputs go back chunk by chunk while the parse
+ * goes on). FALX_ERR_FORMAT when a block fails to inflate (the outputs are then
+ * undefined; falx_bgzf_inflate tells which block); FALX_ERR_INVALID when
+ * the blocks' texts are not end to end. */
+int falx_parse_gz_host(falx_ctx *ctx, const falx_schema *schema, const uint8_t *comp, uint64_t comp_len,
+                       const falx_gz_block *blocks, uint64_t n_blocks, falx_outputs *host_out);
 
 /* Structural index without any allocation (no counterpart in the
  * reference, whose callers are Rust code that allocates freely). For callers

@@ -18,7 +18,9 @@ pytestmark = pytest.mark.gpu
 COLS = [(0, fx.U32), (1, fx.STR), (3, fx.U32), (4, fx.F64), (5, fx.F64)]
 
 
-def parse_host(engine, doc, dialect, cols, tape=False):
+def parse_host(engine, doc, dialect, cols, tape=False, gz=None):
+    """falx_parse_host over `doc`; with gz (a bgzf stream whose text is
+    `doc`), falx_parse_gz_host over it instead."""
     n = len(doc)
     src = np.frombuffer(doc, dtype=np.uint8).copy() if n else np.zeros(1, dtype=np.uint8)
     idx_cap, rows_cap, str_cap = n // 2 + 64, n // 2 + 64, n + 64
@@ -51,8 +53,18 @@ def parse_host(engine, doc, dialect, cols, tape=False):
         out.seps, out.seps_cap = seps.ctypes.data, seps.size
         out.ends, out.ends_cap = ends.ctypes.data, ends.size
     cs = fx.Schema(dialect, cols).to_c()
-    _lib.check(engine.lib.falx_parse_host(engine.ctx, ctypes.byref(cs), ctypes.c_void_p(src.ctypes.data), n,
-                                          ctypes.byref(out)), "falx_parse_host")
+    if gz is None:
+        _lib.check(engine.lib.falx_parse_host(engine.ctx, ctypes.byref(cs), ctypes.c_void_p(src.ctypes.data), n,
+                                              ctypes.byref(out)), "falx_parse_host")
+    else:
+        from falx_gb300 import bgzf
+
+        blocks, total = bgzf.scan(gz)
+        assert total == n
+        comp = np.frombuffer(gz, dtype=np.uint8).copy()
+        _lib.check(engine.lib.falx_parse_gz_host(engine.ctx, ctypes.byref(cs), ctypes.c_void_p(comp.ctypes.data),
+                                                 comp.size, blocks.ctypes.data_as(ctypes.c_void_p), len(blocks),
+                                                 ctypes.byref(out)), "falx_parse_gz_host")
     res = (index[: out.n_index], hcols.rows, keep, [hcols.cols[k].str_len for k in range(len(cols))])
     if tape:
         return res + (seps[: out.n_seps], ends[: out.n_ends], (fb.fields, fb.bytes))
@@ -120,3 +132,74 @@ def test_pipelined_equals_whole_input(engine, kind, dialect, size):
     # and the oracle's tape
     s, e = oracle.parse_tape(doc, dialect)
     assert np.array_equal(got[4], s) and np.array_equal(got[5], e)
+
+
+def same_outputs(got, want, cols):
+    assert np.array_equal(got[0], want[0])
+    assert got[1] == want[1]
+    rows = got[1]
+    words = (rows + 63) // 64
+    for k, (_, t) in enumerate(cols):
+        (v, valid, sd), (w, wvalid, wsd) = got[2][k], want[2][k]
+        assert np.array_equal(valid[:words], wvalid[:words]), k
+        if t == fx.STR:
+            assert got[3][k] == want[3][k]
+            assert np.array_equal(v[: rows + 1], w[: rows + 1]) and bytes(sd[: got[3][k]]) == bytes(wsd[: got[3][k]])
+        else:
+            assert np.array_equal(v[:rows].view(np.uint8), w[:rows].view(np.uint8)), k
+    if len(got) > 4:
+        assert np.array_equal(got[4], want[4]) and np.array_equal(got[5], want[5]) and got[6] == want[6]
+
+
+# bgzf text parsed from host buffers (falx_parse_gz_host): the compressed
+# bytes copied in, the text inflated in device memory; the same outputs as
+# falx_parse_host over the text, in the pipelined form (80 MiB) and the
+# whole-input form (3 MiB).
+@pytest.mark.parametrize("kind,dialect,size", [(gen.CSV_HASH, fx.CSV_HASH, (80 << 20) + 5),
+                                               (gen.ADVERSARIAL, fx.CSV_HASH, 3 << 20),
+                                               (gen.CSV_GEO, fx.CSV, 1 << 20)])
+def test_parse_gz_host_equals_parse_host(engine, kind, dialect, size):
+    from falx_gb300 import bgzf
+
+    doc = bytes(gen.generate(kind, size))
+    comp = bgzf.compress(doc, 6)
+    want = parse_host(engine, doc, dialect, COLS, tape=True)
+    for rep in range(2):  # the second call reuses the compressed-stream buffer and the flags
+        got = parse_host(engine, doc, dialect, COLS, tape=True, gz=comp)
+        same_outputs(got, want, COLS)
+
+
+def test_parse_gz_host_errors(engine):
+    import ctypes
+
+    from falx_gb300 import bgzf
+
+    doc = bytes(gen.generate(gen.CSV_HASH, 2 << 20))
+    comp = bytearray(bgzf.compress(doc, 6))
+    blocks, total = bgzf.scan(bytes(comp))
+    cs = fx.Schema(fx.CSV_HASH, COLS).to_c()
+    out = _lib.falx_outputs()
+    buf = np.frombuffer(bytes(comp), dtype=np.uint8).copy()
+
+    def call(b, data):
+        return engine.lib.falx_parse_gz_host(engine.ctx, ctypes.byref(cs), ctypes.c_void_p(data.ctypes.data),
+                                             data.size, b.ctypes.data_as(ctypes.c_void_p), len(b), ctypes.byref(out))
+
+    # texts not end to end
+    bad = blocks.copy()
+    bad[3]["out_off"] += 1
+    assert call(bad, buf) == _lib.FALX_ERR_INVALID
+    # a corrupt member: FALX_ERR_FORMAT
+    b = blocks[5]
+    comp[int(b["in_off"]) + 3] ^= 0x40
+    comp[int(b["in_off"]) + 9] ^= 0x11
+    comp[int(b["in_off"]) + 17] ^= 0x08
+    broken = np.frombuffer(bytes(comp), dtype=np.uint8).copy()
+    status = bgzf.inflate(engine, bytes(comp), blocks, total, status=True)[1]
+    assert call(blocks, broken) == (_lib.FALX_ERR_FORMAT if status.any() else _lib.FALX_OK)
+    # and the context parses a good stream afterwards
+    got = parse_host(engine, doc, fx.CSV_HASH, COLS, gz=bytes(bgzf.compress(doc, 1)))
+    assert got[1] == parse_host(engine, doc, fx.CSV_HASH, COLS)[1]
+    # an empty stream: no rows
+    empty = parse_host(engine, b"", fx.CSV_HASH, COLS, gz=bgzf.EOF_MEMBER)
+    assert empty[1] == 0 and len(empty[0]) == 0
