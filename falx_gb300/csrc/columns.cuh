@@ -93,6 +93,7 @@ struct ColSmem {
     uint32_t arena_base[kMaxStr];
     uint64_t vbits[kMaxCols][kRecWords];
     uint32_t blk;
+    uint32_t fb_next;  // the next chunk of 32 records for the field-byte / count-sum totals
     unsigned long long red[kWarps][14];
     alignas(16) uint8_t data[kDataWin + 16];  // 16 bytes of slack for word reads near the window end
 };
@@ -448,6 +449,7 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
     const RowSpec &rs = p.rows;
     const uint64_t R0 = (uint64_t)blk * kRecBlock;
     for (int i = tid; i < rs.ncols * kRecWords; i += kThreads) S.vbits[i / kRecWords][i % kRecWords] = 0;
+    if (tid == 0) S.fb_next = 0;
 
     // ---- windows: from the block's first record to its last, computed by
     // every thread from the two tape entries that bound them
@@ -666,20 +668,27 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
                 }
             }
         }
-        if (lane == 0)
-            for (int k = 0; k < 14; k++) S.red[0][k] = 0;
-    } else {
-        // ---- meanwhile warps 1-7: field-byte and count / sum totals of all
-        // the block's records (they need no prefix), warp sums into shared
-        // memory for the block totals at the end
+    }
+    {
+        // ---- field-byte and count / sum totals of all the block's records
+        // (they need no prefix), in chunks of 32 records from a shared
+        // counter: warps 1-7 start at once, warp 0 joins after its
+        // look-back (a fixed split left two warps a third chunk while the
+        // rest waited at the barrier); warp sums into shared memory for the
+        // block totals at the end
         StatAcc acc = {};
         uint32_t fb_fields = 0, fb_bytes = 0;  // below 2^32: the input is shorter than 4 GiB
         uint64_t tx_values = 0, tx_bytes = 0, tx_sum = 0;
         if (rs.want_fb || STATS) {
-            // (the loop is warp-uniform: a warp's lanes take the same number
-            // of records, so the field-byte cleaning can use the whole warp)
-            for (int li = tid - 32; li < kRecBlock; li += kThreads - 32) {
-                const Rec x = make_rec<D>(p, tc, W, E, R0, li);
+            // (the loop is warp-uniform: a warp's lanes take consecutive
+            // records of one chunk, so the field-byte cleaning can use the
+            // whole warp)
+            for (;;) {
+                uint32_t ch = 0;
+                if (lane == 0) ch = atomicAdd(&S.fb_next, 1u);
+                ch = __shfl_sync(0xffffffffu, ch, 0);
+                if (ch >= (uint32_t)(kRecBlock / 32)) break;
+                const Rec x = make_rec<D>(p, tc, W, E, R0, (int)ch * 32 + lane);
                 if (STATS && x.row) {
                     acc.records++;
 #pragma unroll
