@@ -739,19 +739,22 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
         for (int c = 0; c < rs.ncols; c++)
             if (rs.type[c] == 3) static_cast<int32_t *>(rs.values[c])[0] = 0;
     uint32_t okm[kRecPerThread] = {0, 0};  // per record: valid columns
-    for (int c = 0; c < rs.ncols; c++) {
-        const uint32_t f = rs.field[c], ty = rs.type[c];
-        const int k = rs.str_slot[c];
-        const uint32_t abase = ty == 3 ? S.arena_base[k] + S.warp_len[warp][k] : 0u;
-        // one copy of the cell code for both records (a smaller loop body
-        // measured faster than the unrolled pair: instruction fetch)
+    // Records outer, columns inner: a record's fields are picked once, not
+    // once per column (1.95 -> 1.88 ms per GiB); one copy of the cell code
+    // for both records (a smaller loop body measured faster than the
+    // unrolled pair: instruction fetch).
 #pragma unroll 1
-        for (int i = 0; i < kRecPerThread; i++) {
-            const Rec x = i ? rec[1] : rec[0];
+    for (int i = 0; i < kRecPerThread; i++) {
+        const Rec x = i ? rec[1] : rec[0];
+        const uint32_t g = i ? grow[1] : grow[0];
+        uint32_t okb = 0;  // the record's valid columns
+        for (int c = 0; c < rs.ncols; c++) {
+            const uint32_t f = rs.field[c], ty = rs.type[c];
+            const int k = rs.str_slot[c];
+            const uint32_t abase = ty == 3 ? S.arena_base[k] + S.warp_len[warp][k] : 0u;
             if (ty == 3) {
                 // strings: every lane takes part (quoted cells are cleaned by
                 // the whole warp after the plain copies)
-                const uint32_t g = i ? grow[1] : grow[0];
                 const uint32_t pos = abase + (i ? pick(ex[1], 1 + k) : pick(ex[0], 1 + k));
                 uint32_t a = 0, b = 0, o;
                 const bool present = x.row && W.field(x, f, a, b);
@@ -778,12 +781,10 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
                     if (lane == sl) len = cl;
                 }
                 if (x.row && g < rs.rows_cap) static_cast<int32_t *>(rs.values[c])[(uint64_t)g + 1] = (int32_t)(pos + len);
-                if (i) okm[1] |= (uint32_t)present << c;
-                else okm[0] |= (uint32_t)present << c;
+                okb |= (uint32_t)present << c;
                 continue;
             }
             if (!x.row) continue;
-            const uint32_t g = i ? grow[1] : grow[0];
             uint32_t a = 0, b = 0, o;
             const bool present = W.field(x, f, a, b);
             const uint32_t n = b - a;
@@ -822,9 +823,10 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
                     sp[2 * (uint64_t)g + 1] = ok ? b : 0u;
                 }
             }
-            if (i) okm[1] |= (uint32_t)ok << c;
-            else okm[0] |= (uint32_t)ok << c;
+            okb |= (uint32_t)ok << c;
         }
+        if (i) okm[1] = okb;
+        else okm[0] = okb;
     }
     // ---- validity: the warp's rows are consecutive, at most 64 of them;
     // one 64-bit word per column and warp. With every record a row, record
