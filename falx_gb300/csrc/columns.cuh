@@ -671,10 +671,11 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
     }
     {
         // ---- field-byte and count / sum totals of all the block's records
-        // (they need no prefix), in chunks of 32 records from a shared
-        // counter: warps 1-7 start at once, warp 0 joins after its
-        // look-back (a fixed split left two warps a third chunk while the
-        // rest waited at the barrier); warp sums into shared memory for the
+        // (they need no prefix): warps 1-7 take their own two chunks of 32
+        // records (already in registers), then warp 0's two chunks from a
+        // shared counter, which warp 0 joins after its look-back (a fixed
+        // split of all 16 chunks left two warps a third chunk while the rest
+        // waited at the barrier); warp sums into shared memory for the
         // block totals at the end
         StatAcc acc = {};
         uint32_t fb_fields = 0, fb_bytes = 0;  // below 2^32: the input is shorter than 4 GiB
@@ -683,12 +684,17 @@ __device__ __forceinline__ void columns_block(const ColParams &p, const TapeCoun
             // (the loop is warp-uniform: a warp's lanes take consecutive
             // records of one chunk, so the field-byte cleaning can use the
             // whole warp)
-            for (;;) {
-                uint32_t ch = 0;
-                if (lane == 0) ch = atomicAdd(&S.fb_next, 1u);
-                ch = __shfl_sync(0xffffffffu, ch, 0);
-                if (ch >= (uint32_t)(kRecBlock / 32)) break;
-                const Rec x = make_rec<D>(p, tc, W, E, R0, (int)ch * 32 + lane);
+            for (int it = warp == 0 ? kRecPerThread : 0;; it++) {
+                Rec x;
+                if (it < kRecPerThread) {
+                    x = it ? rec[1] : rec[0];
+                } else {
+                    uint32_t ch = 0;
+                    if (lane == 0) ch = atomicAdd(&S.fb_next, 1u);
+                    ch = __shfl_sync(0xffffffffu, ch, 0);
+                    if (ch >= (uint32_t)kRecPerThread) break;  // warp 0's chunks
+                    x = make_rec<D>(p, tc, W, E, R0, (int)ch * 32 + lane);
+                }
                 if (STATS && x.row) {
                     acc.records++;
 #pragma unroll
