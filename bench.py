@@ -93,7 +93,7 @@ class Clocks:
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons}
 
 
-STEP_KERNELS = ["index_kernel (index + tape)", "columns_kernel"]
+STEP_KERNELS = ["index_pass_kernel (index + tape)", "columns_kernel"]
 
 
 def measured_traffic(n):
