@@ -50,3 +50,30 @@ DIALECT_ALPHABETS = {
 
 def random_doc(rng, alphabet, length):
     return bytes(alphabet[rng.next() % len(alphabet)] for _ in range(length))
+
+
+def reference_shape_ndjson(rng, lines):
+    """NDJSON in the shape of the reference's id + score fixture
+    (tests/ndjson_id_score.rs:5-19): each line starts `{"id":<int>`, then
+    a name string, a tags array and `"nested":{"score":<int>,...}`, then a
+    note. Names and notes carry escaped quotes and backslashes, braces and
+    decoy keys ("id", "score") inside strings; blank and CR-ended lines are
+    mixed in. The reference's literal sink accepts every such line, so its
+    records and sum are the known answer for a JSON-aware sink."""
+    decoys = [b'plain', b'quoted \\" id\\":999', b'slash \\\\ nested score\\":123', b'brace } inside',
+              b'{\\"id\\":5}', b'],\\"nested\\":{\\"score\\":1}', b'tab\\tand\\nnewline', b'']
+    out = bytearray()
+    for _ in range(lines):
+        if rng.next() % 17 == 0:
+            out += b"\n" if rng.next() % 2 else b"\r\n"
+        ident = rng.next() % 2_000_000_000 - 1_000_000_000
+        score = rng.next() % 200_001 - 100_000
+        name = decoys[rng.next() % len(decoys)]
+        note = decoys[rng.next() % len(decoys)]
+        ntags = rng.next() % 4
+        tags = b",".join(b'"t%d"' % (rng.next() % 100) for _ in range(ntags))
+        ok = b"true" if rng.next() % 2 else b"false"
+        out += (b'{"id":%d,"name":"%s","tags":[%s],"nested":{"score":%d,"ok":%s},"note":"%s"}'
+                % (ident, name, tags, score, ok, note))
+        out += b"\r\n" if rng.next() % 11 == 0 else b"\n"
+    return bytes(out)

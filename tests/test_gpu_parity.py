@@ -222,6 +222,19 @@ def test_ndjson_known_answer(engine):
     assert oracle.ndjson_literal(doc) == (3, 62)
 
 
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_ndjson_reference_shape_known_answers(engine, seed):
+    # known answers from the reference's literal algorithm (ndjson.rs:662-880)
+    # on lines of its fixture's shape, many of them across tile boundaries
+    from conftest import reference_shape_ndjson
+
+    doc = reference_shape_ndjson(Rng(seed), 60000)
+    records, total = oracle.ndjson_literal(doc)
+    st = engine.ndjson_id_score(doc)
+    assert st.records == records
+    assert st.total_e6 == total * 10**6
+
+
 def test_ndjson_generated(engine):
     doc = gen.generate(gen.NDJSON, 8 << 20)
     st = engine.ndjson_id_score(doc)

@@ -97,3 +97,18 @@ def test_parallel_port_matches_serial(kind, dialect):
                     assert g == v
                 else:
                     assert np.array_equal(np.asarray(g).view(np.uint8), np.asarray(v).view(np.uint8))
+
+
+def test_ndjson_json_sink_matches_literal_sink_on_reference_shape():
+    # the JSON-aware restatement against the reference's literal algorithm
+    # (ndjson.rs:662-880, oracle.ndjson_literal) on lines of the reference
+    # fixture's shape, where both must accept every line
+    from conftest import Rng, reference_shape_ndjson
+
+    for seed in (1, 2, 3):
+        doc = reference_shape_ndjson(Rng(seed), 3000)
+        lit = oracle.ndjson_literal(doc)
+        js = oracle.ndjson_json(doc)
+        assert lit is not None and js is not None
+        assert js["records"] == lit[0]
+        assert js["total_e6"] == lit[1] * 10**6
