@@ -5,6 +5,7 @@ the parse); the whole-input form (FALX_OPT_PIPELINE 0) must give the same
 outputs."""
 
 import ctypes
+import random
 
 import numpy as np
 import pytest
@@ -203,3 +204,49 @@ def test_parse_gz_host_errors(engine):
     # an empty stream: no rows
     empty = parse_host(engine, b"", fx.CSV_HASH, COLS, gz=bgzf.EOF_MEMBER)
     assert empty[1] == 0 and len(empty[0]) == 0
+
+
+def test_parse_gz_host_corrupt_member_at_pipeline_size(engine):
+    # a member that fails to inflate in a stream large enough for the
+    # pipelined parse: FALX_ERR_FORMAT (the parse ran over whatever the text
+    # buffer held), then the same context parses a good stream correctly
+    import ctypes
+
+    from falx_gb300 import bgzf
+
+    doc = bytes(gen.generate(gen.CSV_HASH, 72 << 20))
+    comp = bytearray(bgzf.compress(doc, 1))
+    blocks, total = bgzf.scan(bytes(comp))
+    rng = random.Random(5)
+    for k in rng.sample(range(len(blocks)), 8):
+        b = blocks[k]
+        for _ in range(4):
+            comp[int(b["in_off"]) + rng.randrange(int(b["in_len"]))] ^= 1 << rng.randrange(8)
+    status = bgzf.inflate(engine, bytes(comp), blocks, total, status=True)[1]
+    assert status.any()  # (at least one of the damaged members fails)
+    cs = fx.Schema(fx.CSV_HASH, COLS).to_c()
+    hcols = _lib.falx_columns()
+    rows_cap = total // 8
+    keep = []
+    for k, (_, t) in enumerate(COLS):
+        v = np.zeros(rows_cap + 1, dtype=np.float64)  # 8 bytes a row covers every type
+        valid = np.zeros((rows_cap + 63) // 64, dtype=np.uint64)
+        hcols.cols[k].values = v.ctypes.data
+        hcols.cols[k].valid = valid.ctypes.data
+        if t == fx.STR:
+            sd = np.zeros(total, dtype=np.uint8)
+            hcols.cols[k].str_data = sd.ctypes.data
+            hcols.cols[k].str_cap = sd.size
+            keep.append(sd)
+        keep += [v, valid]
+    hcols.rows_cap = rows_cap
+    out = _lib.falx_outputs()
+    out.columns = ctypes.pointer(hcols)
+    data = np.frombuffer(bytes(comp), dtype=np.uint8).copy()
+    rc = engine.lib.falx_parse_gz_host(engine.ctx, ctypes.byref(cs), ctypes.c_void_p(data.ctypes.data), data.size,
+                                       blocks.ctypes.data_as(ctypes.c_void_p), len(blocks), ctypes.byref(out))
+    assert rc == _lib.FALX_ERR_FORMAT
+    good = bgzf.compress(doc[: 66 << 20], 1)
+    got = parse_host(engine, doc[: 66 << 20], fx.CSV_HASH, COLS, gz=good)
+    want = parse_host(engine, doc[: 66 << 20], fx.CSV_HASH, COLS)
+    same_outputs(got, want, COLS)
